@@ -1,0 +1,366 @@
+"""Benchmark: IDG grid + degrid (w-stacked) on the 3072^2 workload.
+
+One step = IDG.GridW (gridder, subgrid IFFT, w-stack adder) + IDG.DeGridW (splitter,
+subgrid FFT, degridder) over the whole synthetic observation: 2016 baselines x 2000
+times x 16 channels (64.5M visibilities, 42M of them gridded after the partitioner's
+channel-span drop), N = 3072, S = 32, 8 w layers.  The metric counts visibilities
+processed by the gridder plus the degridder per second.
+
+  value : device-resident buffers (C ABI device entry points), CUDA events on the plan's stream
+  e2e   : the reference-facing host API (IDG.GridW / IDG.DeGridW with Complex[...] host
+          arrays in pinned memory), host<->device copies inside the timed region
+  --impl reference : the CPU restatement of the reference gridder (oracle/) on all host cores
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import __graft_entry__ as entry  # noqa: E402
+
+WORKLOAD = "meerkat_3072"
+METRIC = "Mvis/s grid+degrid at 3072², TC split-precision vs FP32, rel-L2 err vs FP64"
+MODES = {"fp32": 0, "tc_bf16x3": 1, "tc_fp16x3": 2}
+
+
+def dist_info():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(self.gpu)], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+def traffic_per_launch(kernel):
+    """Per-launch DRAM bytes from the committed ncu summary (profiles/traffic_per_launch.txt)."""
+    p = os.path.join(ROOT, "profiles", "traffic_per_launch.txt")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        for line in f:
+            parts = line.split()
+            if len(parts) >= 3 and not line.startswith("#") and parts[0] == kernel and parts[1] == WORKLOAD:
+                return float(parts[2])
+    return None
+
+
+def pick_sample(subs, nch, target_vis, seed=0):
+    rng = np.random.default_rng(seed)
+    take, tot = [], 0
+    for i in rng.permutation(len(subs)):
+        take.append(i)
+        tot += int(subs[i]["time_sample_count"]) * nch
+        if tot >= target_vis:
+            break
+    return subs[np.sort(np.array(take, dtype=np.int64))], tot
+
+
+def cpu_reference_step(oracle, cd, sample, obs, model_grid):
+    """One sample of the reference gridder restated on the CPU: GridW + DeGridW of the sample."""
+    layers = oracle.idg_grid_w(cd, sample, obs.vis, obs.uvw, obs.frequencies)
+    vis, _ = oracle.idg_degrid(cd, sample, model_grid, obs.uvw, obs.frequencies, wstack=True)
+    return layers, vis
+
+
+def calibrate_cpu_sample(oracle, cd, subs, obs, model_grid, budget_s):
+    """A seeded subgrid sample whose CPU grid+degrid takes about budget_s (from a short pilot)."""
+    nch = obs.vis.shape[2]
+    pts = []
+    for n in (40000, 160000):  # two pilots: fixed cost (w-layer allocation, shifts) + per-visibility cost
+        sample, nv = pick_sample(subs, nch, n, seed=1)
+        t0 = time.perf_counter()
+        cpu_reference_step(oracle, cd, sample, obs, model_grid)
+        pts.append((nv, time.perf_counter() - t0))
+    (n1, t1), (n2, t2) = pts
+    per_vis = max((t2 - t1) / max(n2 - n1, 1), 1e-9)
+    fixed = max(t1 - per_vis * n1, 0.0)
+    target = int(max(budget_s - fixed, 0.5 * budget_s) / per_vis)
+    sample, nv = pick_sample(subs, nch, target)
+    return sample, nv, fixed
+
+
+def load_oracle():
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle  # noqa: E402  (CPU baseline leg only)
+    oracle.lib()
+    return oracle
+
+
+def run_reference(args):
+    ws, rank, _ = dist_info()
+    if rank != 0:
+        return 0
+    synth = entry._load_module(entry.PKG_NAME + ".synth", os.path.join(entry.PKG_DIR, "synth.py"))
+    oracle = load_oracle()
+    obs, cd = synth.build(WORKLOAD)
+    subs = oracle.partition(cd, obs.uvw, obs.frequencies)
+    model_grid = oracle.fft_forward_float(oracle.shift(obs.model_image.astype(np.float32)))
+    cores = oracle.num_threads()
+    budget = max(3.0, min(20.0, 120.0 / max(1, args.steps + args.warmup)))
+    sample, nv, _ = calibrate_cpu_sample(oracle, cd, subs, obs, model_grid, budget)
+    for _ in range(args.warmup):
+        cpu_reference_step(oracle, cd, sample, obs, model_grid)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        cpu_reference_step(oracle, cd, sample, obs, model_grid)
+        times.append(time.perf_counter() - t0)
+    t = sum(times)
+    value = 2 * nv * args.steps / t / 1e6
+    gridded = int(subs["time_sample_count"].sum()) * obs.vis.shape[2]
+    desc = (f"{len(sample)} of {len(subs)} subgrids ({nv} of {gridded} gridded visibilities), seeded; "
+            f"GridW + DeGridW of the sample, FP64, {cores} OpenMP threads")
+    out = {"metric": METRIC, "value": value, "unit": "Mvis/s", "n_gpus": args.gpus, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, 3072^2 workload)",
+           "impl": "reference",
+           "config": {"workload": "3072^2 IDG grid+degrid: 2016 bl x 2000 t x 16 ch, S=32, W=8",
+                      "sample": desc},
+           "cpu_baseline": {"value": value, "unit": "Mvis/s", "cores": cores, "kind": "port", "sample": desc},
+           "e2e": {"value": value, "unit": "Mvis/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--mode", default="auto", choices=["auto"] + list(MODES))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+
+    ws, rank, local = dist_info()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    pkg = entry.load_package()
+    synth = entry._load_module(entry.PKG_NAME + ".synth", os.path.join(entry.PKG_DIR, "synth.py"))
+
+    wl = synth.scaled_workload(WORKLOAD, seed=synth.WORKLOADS[WORKLOAD]["obs"]["seed"] + rank)
+    obs, cd = synth.build(wl)
+    c = pkg.GriddingConstants.from_dict(cd)
+    part = pkg.Partitioner.CreatePartition(c, obs.uvw, obs.frequencies)
+    plan = part.plan
+    info = plan.info()
+    mode_name = args.mode
+    if mode_name == "auto":
+        mode_name = "fp32"
+        for m in ("tc_bf16x3",):
+            try:
+                plan.set_mode(MODES[m])
+                mode_name = m
+                break
+            except pkg.P9IDGError:
+                pass
+    plan.set_mode(MODES[mode_name])
+
+    stream = torch.cuda.Stream()
+    plan.set_stream(stream.cuda_stream)
+    N, W = cd["grid_size"], cd["wlayer_count"]
+    model_img = obs.model_image.astype(np.float32)
+    model_grid = pkg.FFT.Forward(np.fft.ifftshift(model_img) if N % 2 == 0 else model_img)
+    with torch.cuda.stream(stream):
+        d_vis = torch.from_numpy(obs.vis.astype(np.complex64)).cuda()
+        d_layers = torch.empty((W, N, N), dtype=torch.complex64, device="cuda")
+        d_grid = torch.from_numpy(model_grid.astype(np.complex64)).cuda()
+        d_out = torch.empty_like(d_vis)
+    stream.synchronize()
+
+    def step():
+        plan.grid_w_device(d_vis.data_ptr(), d_layers.data_ptr())
+        plan.degrid_w_device(d_grid.data_ptr(), d_out.data_ptr())
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    plan.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    plan.reset_timing()
+    plan.enable_timing(True)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    e1.synchronize()
+    plan.synchronize()
+    clk = clocks.stop()
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    stages = plan.stage_times()
+    plan.enable_timing(False)
+    if ws > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    gridded = info["gridded_visibilities"]
+    value = ws * 2 * gridded * args.steps / (ms * 1e-3) / 1e6
+    launches = sum(n for (_, n) in stages.values()) - stages["h2d"][1] - stages["d2h"][1]
+
+    # roofline of the dominant kernel
+    S = cd["subgrid_size"]
+    peaks, peak_src = measured_peaks()
+    kern = max(("gridder", "degridder"), key=lambda k: stages[k][0])
+    kt_ms = stages[kern][0] / max(1, stages[kern][1])
+    if mode_name == "fp32":
+        sincos_peak, fma_peak = pkg.measure_sincos_peak()
+        achieved = gridded * S * S / (kt_ms * 1e-3) / 1e9
+        roofline = {"bound": "sfu", "achieved": achieved, "peak": sincos_peak / 1e9, "unit": "Gsincos/s",
+                    "frac": achieved / (sincos_peak / 1e9), "traffic": traffic_per_launch(kern + "_fp32"),
+                    "kernel": kern + "_fp32", "peak_source": "measured on this GPU (hardware sincos probe loop)",
+                    "work_per_launch": f"{gridded} visibilities x {S * S} pixels, one sincos + 10 flop each"}
+    else:
+        achieved = gridded * 10 * S * S / (kt_ms * 1e-3) / 1e12
+        roofline = {"bound": "tensor", "achieved": achieved, "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
+                    "frac": achieved / peaks["bf16_tflops"], "traffic": traffic_per_launch(kern + "_" + mode_name),
+                    "kernel": kern + "_" + mode_name, "peak_source": f"{peak_src} bf16 dense (MEASURED_PEAKS.json)",
+                    "work_per_launch": f"{gridded} visibilities x {S * S} pixels x 10 algorithmic flop"}
+    stage_ms = {k: round(v[0] / max(1, v[1]), 4) for k, v in stages.items() if v[1]}
+
+    # e2e through the reference-facing host API with pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        pin = lambda shape, dt: torch.empty(shape, dtype=dt, pin_memory=True).numpy()  # noqa: E731
+        h_vis = pin(obs.vis.shape, torch.complex128)
+        h_vis[...] = obs.vis
+        h_uvw = pin(obs.uvw.shape, torch.float64)
+        h_uvw[...] = obs.uvw
+        h_layers = pin((W, N, N), torch.complex128)
+        h_grid = pin((N, N), torch.complex128)
+        h_grid[...] = model_grid
+        plan.set_stream(0)
+        pkg.IDG.GridW(c, part, h_vis, h_uvw, obs.frequencies)  # warm-up of the host path buffers
+        pkg.IDG.DeGridW(c, part, h_grid, h_uvw, obs.frequencies)
+        steps_e2e = max(1, min(args.steps, 3))
+        t0 = time.perf_counter()
+        for _ in range(steps_e2e):
+            lay = pkg.IDG.GridW(c, part, h_vis, h_uvw, obs.frequencies)
+            v = pkg.IDG.DeGridW(c, part, h_grid, h_uvw, obs.frequencies)
+        t_e2e = time.perf_counter() - t0
+        del lay, v
+        nvis = obs.vis.size
+        h2d = nvis * 16 + 2 * obs.uvw.nbytes + N * N * 16
+        d2h = W * N * N * 16 + N * N * 16 + nvis * 16
+        e2e = {"value": ws * 2 * gridded * steps_e2e / t_e2e / 1e6, "unit": "Mvis/s",
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+               "note": "IDG.GridW + IDG.DeGridW host API, Complex(double) arrays in pinned host memory, "
+                       "wall clock incl. H2D/D2H and complex128<->complex64 conversion"}
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        oracle = load_oracle()
+        subs = plan.subgrids()
+        mg = model_grid
+        sample, nv, _ = calibrate_cpu_sample(oracle, cd, subs, obs, mg, 12.0)
+        t0 = time.perf_counter()
+        layers_ref, vis_ref = cpu_reference_step(oracle, cd, sample, obs, mg)
+        t_cpu = time.perf_counter() - t0
+        # accuracy of the GPU path on the same sample (plan restricted to the sampled subgrids)
+        sp = pkg.plan_from_subgrids(c, sample, obs.uvw, obs.frequencies)
+        sp.set_mode(MODES[mode_name])
+        spart = pkg.Partition([[]], sp)
+        lay_gpu = pkg.IDG.GridW(c, spart, obs.vis, obs.uvw, obs.frequencies)
+        vis_gpu = pkg.IDG.DeGridW(c, spart, mg.copy(), obs.uvw, obs.frequencies)
+        rl = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))  # noqa: E731
+        cpu = {"value": 2 * nv / t_cpu / 1e6, "unit": "Mvis/s", "cores": oracle.num_threads(), "kind": "port",
+               "sample": f"{len(sample)} of {len(subs)} subgrids ({nv} of {gridded} gridded visibilities), "
+                         f"GridW + DeGridW of the sample in FP64",
+               "rel_l2_vs_fp64": {"grid_w": rl(lay_gpu, layers_ref), "degrid_w": rl(vis_gpu, vis_ref),
+                                  "mode": mode_name, "visibilities": nv}}
+
+    if rank == 0:
+        out = {"metric": METRIC, "value": value, "unit": "Mvis/s", "n_gpus": ws, "steps": args.steps,
+               "warmup": max(3, args.warmup), "ms_per_step": ms / args.steps, "higher_is_better": True,
+               "scaling": "weak", "vs_baseline": None, "dtype": "f32" if mode_name == "fp32" else mode_name,
+               "data": "synthetic (seeded; stands in for the reference's MeerKAT FITS data, absent)",
+               "config": {"workload": "3072^2 IDG grid+degrid: 2016 bl x 2000 t x 16 ch (64.5M vis), S=32, W=8",
+                          "mode": mode_name, "input_visibilities": info["input_visibilities"],
+                          "gridded_visibilities": gridded, "subgrids": info["num_subgrids"],
+                          "l2_flush": "inputs larger than L2 (vis 1.03 GB, layers 604 MB complex64)",
+                          "value_counts": "gridded visibilities x 2 (gridder + degridder) per step",
+                          "per_stage_ms": stage_ms},
+               "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
+               "clocks": clk}
+        print(json.dumps(out), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

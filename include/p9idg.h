@@ -1,0 +1,203 @@
+/*
+ * p9idg.h -- C ABI of the GB300 (sm_103a) image-domain gridder with w-stacking.
+ *
+ * Drop-in for the gridding path of lord-blueberry/p9-distributed-reconstruction
+ * (C#, project "Core", namespace Core.ImageDomainGridder).  Every entry point
+ * names the reference member it replaces (file:line, paths inside
+ * Distributed-Reconstruction/).  A C# caller binds these with P/Invoke; the
+ * arrays it passes are its own pinned, row-major multidimensional arrays:
+ *
+ *   double[nbl, nt, 3]      uvw          metres
+ *   double[nch]             frequencies  Hz
+ *   Complex[nbl, nt, nch]   vis          interleaved (re, im) doubles
+ *   bool[nbl, nt, nch]      flags        one byte per sample, nonzero = flagged
+ *   Complex[N, N]           grid         interleaved (re, im) doubles
+ *   List<Complex[N, N]>     w layers     passed as one [W][N][N] block
+ *
+ * Callers own every array.  The library owns plans, device memory, CUDA
+ * streams and cuFFT plans.  Calls on distinct plans may run from different
+ * threads; a single plan is not re-entrant.  All entry points return a status;
+ * p9idg_last_error() gives a thread-local message for the last failure.
+ */
+#ifndef P9IDG_H
+#define P9IDG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t p9idg_status;
+
+enum {
+    P9IDG_OK = 0,
+    P9IDG_INVALID_ARGUMENT = 1,     /* bad sizes/pointers; also the reference's IndexOutOfRange cases */
+    P9IDG_CANNOT_PLACE = 2,         /* "could not place (all) visibilities on subgrid" Partitioner.cs:86,91 */
+    P9IDG_SUBGRID_OUT_OF_GRID = 3,  /* "subgrid falls not within grid" Partitioner.cs:118 */
+    P9IDG_INVALID_GRID = 4,         /* "invalid grid" Adder.cs:49 */
+    P9IDG_OUT_OF_MEMORY = 5,
+    P9IDG_CUDA_ERROR = 6,
+    P9IDG_NO_DEVICE = 7,
+    P9IDG_UNSUPPORTED = 8,          /* e.g. tensor-core mode for a subgrid size it does not cover */
+    P9IDG_DEVICE_CHECK_FAILED = 9   /* a kernel's own bounds check tripped (no access was made) */
+};
+
+/* Gridding precision of the gridder/degridder kernels. */
+enum {
+    P9IDG_MODE_FP32 = 0,      /* FP32 sincos + FMA, FP64 per-visibility phase argument */
+    P9IDG_MODE_TC_BF16X3 = 1, /* tensor cores, BF16 hi+lo split (3 products), FP32 accumulation */
+    P9IDG_MODE_TC_FP16X3 = 2  /* tensor cores, FP16 hi+lo split (3 products), FP32 accumulation */
+};
+
+/* GriddingConstants (Core/ImageDomainGridder/GriddingConstants.cs:33-52).
+ * scale_arcsec is the cell size in radians, stored as float like the
+ * reference's ScaleArcSec.  WStepLambda is not a field: the reference never
+ * assigns it (GriddingConstants.cs:25), so the w offset of every subgrid is 0.
+ * The subgrid taper (SubgridSpheroidal) is the identity unless
+ * p9idg_plan_set_taper installs one. */
+typedef struct p9idg_params {
+    int64_t vis_count;      /* VisibilitiesCount: normalisation of the image FFTs */
+    int32_t grid_size;      /* GridSize N */
+    int32_t subgrid_size;   /* SubgridSize S */
+    int32_t kernel_size;    /* KernelSize (partitioner margin) */
+    int32_t max_timesteps;  /* MaxTimestepsPerSubgrid */
+    float scale_arcsec;     /* ScaleArcSec (radians per cell) */
+    int32_t wlayer_count;   /* WLayerCount */
+    double wstep;           /* WStep (wavelengths per w layer; 0 = no w binning) */
+} p9idg_params;
+
+/* Subgrid (Core/ImageDomainGridder/Subgrid.cs:15-24).  baseline_idx is the
+ * index of the baseline list the subgrid belongs to; the reference gridder
+ * indexes uvw/vis with that list index (Gridder.cs:28,58). */
+typedef struct p9idg_subgrid {
+    int32_t baseline_idx;
+    int32_t time_sample_start;
+    int32_t time_sample_count;
+    int32_t u_pixel;
+    int32_t v_pixel;
+    int32_t w_lambda;       /* w layer index (may be negative) */
+} p9idg_subgrid;
+
+typedef struct p9idg_plan p9idg_plan;
+
+/* Summary of a plan (counts over the subgrid list). */
+typedef struct p9idg_plan_info {
+    int64_t num_subgrids;
+    int64_t input_visibilities;    /* nbl * nt * nch */
+    int64_t gridded_visibilities;  /* visibilities covered by subgrids (the partitioner drops some) */
+    int64_t work_items;            /* (subgrid, time-chunk) units the gridder kernels process */
+    int32_t nbl, nt, nch;
+    int32_t mode;
+} p9idg_plan_info;
+
+/* ---------------- plans: Partitioner ---------------- */
+
+/* Partitioner.CreatePartition (Core/ImageDomainGridder/Partitioner.cs:20-125).
+ * Builds the subgrid list on the host (bit-identical to the reference's
+ * integer output) and uploads uvw, frequencies and the work list to the GPU. */
+p9idg_status p9idg_plan_create(const p9idg_params *c, const double *uvw, int32_t nbl, int32_t nt,
+                               const double *frequencies, int32_t nch, p9idg_plan **out);
+
+/* A plan from a caller-built List<List<Subgrid>> flattened in list order
+ * (the shape IDG.Grid/DeGrid/GridW/DeGridW receive, IDG.cs:12,22,32,42). */
+p9idg_status p9idg_plan_create_from_subgrids(const p9idg_params *c, const p9idg_subgrid *subgrids, int64_t nsub,
+                                             const double *uvw, int32_t nbl, int32_t nt,
+                                             const double *frequencies, int32_t nch, p9idg_plan **out);
+
+p9idg_status p9idg_plan_num_subgrids(const p9idg_plan *plan, int64_t *n);
+/* Copies the subgrid list (reference order: baseline-major, then time). */
+p9idg_status p9idg_plan_get_subgrids(const p9idg_plan *plan, p9idg_subgrid *out, int64_t capacity);
+p9idg_status p9idg_plan_get_info(const p9idg_plan *plan, p9idg_plan_info *out);
+/* Selects the gridder/degridder kernels (P9IDG_MODE_*). */
+p9idg_status p9idg_plan_set_mode(p9idg_plan *plan, int32_t mode);
+/* Subgrid taper float[S][S] applied by gridder and degridder (GriddingConstants.SubgridSpheroidal,
+ * Gridder.cs:76,111); NULL restores the identity taper the reference uses. */
+p9idg_status p9idg_plan_set_taper(p9idg_plan *plan, const float *taper);
+/* Runs the plan's work on a caller's cudaStream_t (NULL = the plan's own stream). */
+p9idg_status p9idg_plan_set_stream(p9idg_plan *plan, void *cuda_stream);
+p9idg_status p9idg_plan_get_stream(const p9idg_plan *plan, void **cuda_stream);
+void p9idg_plan_destroy(p9idg_plan *plan);
+
+/* ---------------- IDG facade, host arrays (Core/ImageDomainGridder/IDG.cs) ---------------- */
+/* uvw may be NULL to reuse the uvw the plan was created with. */
+
+/* IDG.Grid (IDG.cs:12-20): Gridder.Forward, SubgridFFT.Forward, Adder.Add, FFT.Shift.  grid_out Complex[N,N]. */
+p9idg_status p9idg_grid(p9idg_plan *plan, const double *vis, const double *uvw, double *grid_out);
+/* IDG.DeGrid (IDG.cs:22-30).  Like the reference, FFT.Shift is applied to grid_io in place. */
+p9idg_status p9idg_degrid(p9idg_plan *plan, double *grid_io, const double *uvw, double *vis_out);
+/* IDG.GridW (IDG.cs:32-40): AdderWStack.Add into W layers, each FFT.Shift-ed.  layers_out Complex[W][N,N]. */
+p9idg_status p9idg_grid_w(p9idg_plan *plan, const double *vis, const double *uvw, double *layers_out);
+/* IDG.DeGridW (IDG.cs:42-50).  FFT.Shift is applied to grid_io in place. */
+p9idg_status p9idg_degrid_w(p9idg_plan *plan, double *grid_io, const double *uvw, double *vis_out);
+/* IDG.GridPSF (IDG.cs:52-66): IDG.Grid of unit visibilities where not flagged. */
+p9idg_status p9idg_grid_psf(p9idg_plan *plan, const double *uvw, const uint8_t *flags, double *grid_out);
+/* IDG.ToImage (IDG.cs:68-83): Grid, FFT.Backward(grid, VisibilitiesCount), FFT.Shift.  image_out double[N,N]. */
+p9idg_status p9idg_to_image(p9idg_plan *plan, const double *vis, const double *uvw, double *image_out);
+/* IDG.CalculatePSF (IDG.cs:85-114). */
+p9idg_status p9idg_calculate_psf(p9idg_plan *plan, const double *uvw, const uint8_t *flags, double *psf_out);
+
+/* ---------------- FFT.cs, host arrays (Core/FFT.cs) ---------------- */
+
+/* FFT.WStackIFFTFloat (FFT.cs:188-215): sum over layers of Re(IFFT(layer)) / visCount, float[N,N]. */
+p9idg_status p9idg_wstack_ifft_float(const double *layers, int32_t nlayers, int32_t n, int64_t vis_count,
+                                     float *image_out);
+/* FFT.Forward(float[,] image, double norm) (FFT.cs:99-117): unnormalised forward FFT / norm. */
+p9idg_status p9idg_fft_forward_float(const float *image, int32_t n, double norm, double *grid_out);
+/* FFT.BackwardFloat(Complex[,] image, double norm) (FFT.cs:139-157): Re(IFFT) / norm. */
+p9idg_status p9idg_fft_backward_float(const double *grid, int32_t n, double norm, float *image_out);
+/* FFT.Shift (FFT.cs:221-264): in-place quadrant swap of a square [n][n] array, elem_bytes 4, 8 or 16. */
+p9idg_status p9idg_fft_shift(void *array, int32_t n, int32_t elem_bytes);
+
+/* ---------------- device-resident interface (HBM buffers, complex64 = float2) ---------------- */
+/* These run asynchronously on the plan's stream; p9idg_synchronize waits and
+ * reports kernel-side check failures.  uvw and frequencies are the plan's. */
+
+/* Gridder + subgrid IFFT + w-stack adder: vis complex64[nbl][nt][nch] -> layers complex64[W][N][N]
+ * (already FFT.Shift-ed, as IDG.GridW returns them).  The layers are overwritten. */
+p9idg_status p9idg_grid_w_device(p9idg_plan *plan, const void *d_vis, void *d_layers);
+/* Splitter + subgrid FFT + degridder: grid complex64[N][N] as passed to IDG.DeGridW (not shifted;
+ * the shift is folded into the splitter and the device grid is left unchanged) -> vis complex64. */
+p9idg_status p9idg_degrid_w_device(p9idg_plan *plan, const void *d_grid, void *d_vis);
+/* Non-w variants (IDG.Grid / IDG.DeGrid): one complex64[N][N] grid. */
+p9idg_status p9idg_grid_device(p9idg_plan *plan, const void *d_vis, void *d_grid);
+p9idg_status p9idg_degrid_device(p9idg_plan *plan, const void *d_grid, void *d_vis);
+/* FFT.WStackIFFTFloat (+ the caller's FFT.Shift when shift != 0) on device layers: float image[N][N]. */
+p9idg_status p9idg_wstack_image_device(p9idg_plan *plan, const void *d_layers, float *d_image, int32_t shift);
+p9idg_status p9idg_synchronize(p9idg_plan *plan);
+
+/* ---------------- stage timing (CUDA events on the plan's stream) ---------------- */
+
+enum {
+    P9IDG_STAGE_GRIDDER = 0,
+    P9IDG_STAGE_SUBGRID_IFFT_ADD = 1,
+    P9IDG_STAGE_SPLIT_SUBGRID_FFT = 2,
+    P9IDG_STAGE_DEGRIDDER = 3,
+    P9IDG_STAGE_LAYER_FFT = 4,
+    P9IDG_STAGE_H2D = 5,
+    P9IDG_STAGE_D2H = 6,
+    P9IDG_STAGE_CONVERT = 7,
+    P9IDG_NUM_STAGES = 8
+};
+
+p9idg_status p9idg_plan_enable_timing(p9idg_plan *plan, int32_t on);
+/* Accumulated milliseconds and launch counts per stage since the last reset (synchronises). */
+p9idg_status p9idg_plan_stage_times(p9idg_plan *plan, double *ms, int64_t *launches);
+p9idg_status p9idg_plan_reset_timing(p9idg_plan *plan);
+
+/* ---------------- misc ---------------- */
+
+const char *p9idg_last_error(void);
+const char *p9idg_version(void);
+/* Number of visible CUDA devices (0 when none); does not create a context. */
+int32_t p9idg_device_count(void);
+/* Measured FP32 sincos throughput of the current device (sincos per second) from a short
+ * on-device loop of the intrinsic the FP32 kernels use; the FP32/SFU roofline denominator. */
+p9idg_status p9idg_measure_sincos_peak(double *sincos_per_s, double *fma_per_s);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* P9IDG_H */

@@ -1,0 +1,15 @@
+"""GB300-native (sm_103a) image-domain gridder with w-stacking.
+
+Drop-in for the gridding path of lord-blueberry/p9-distributed-reconstruction
+(Core.ImageDomainGridder + the Core.FFT members it uses).  The compute lives in
+libp9idg.so (CUDA kernels + C ABI, include/p9idg.h); this package is the host-side
+mirror of the reference API over that ABI.
+"""
+from . import _native
+from ._native import (MODE_FP32, MODE_TC_BF16X3, MODE_TC_FP16X3, NativeLibraryMissing, STAGES)
+from .idg import (FFT, IDG, GriddingConstants, P9IDGError, Partition, Partitioner, Plan, Subgrid, SUBGRID_DTYPE,
+                  device_count, measure_sincos_peak, plan_from_subgrids)
+
+__all__ = ["FFT", "IDG", "GriddingConstants", "P9IDGError", "Partition", "Partitioner", "Plan", "Subgrid",
+           "SUBGRID_DTYPE", "MODE_FP32", "MODE_TC_BF16X3", "MODE_TC_FP16X3", "NativeLibraryMissing", "STAGES",
+           "device_count", "measure_sincos_peak", "plan_from_subgrids"]

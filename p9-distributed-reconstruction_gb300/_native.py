@@ -1,0 +1,113 @@
+"""ctypes binding of libp9idg.so (declarations mirror include/p9idg.h).
+
+The library is the product: there is no fallback.  If it is missing, loading raises
+NativeLibraryMissing; compute calls on a machine without a GPU return P9IDG_NO_DEVICE.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libp9idg.so")
+
+OK = 0
+INVALID_ARGUMENT = 1
+CANNOT_PLACE = 2
+SUBGRID_OUT_OF_GRID = 3
+INVALID_GRID = 4
+OUT_OF_MEMORY = 5
+CUDA_ERROR = 6
+NO_DEVICE = 7
+UNSUPPORTED = 8
+DEVICE_CHECK_FAILED = 9
+
+MODE_FP32 = 0
+MODE_TC_BF16X3 = 1
+MODE_TC_FP16X3 = 2
+
+STAGES = ["gridder", "subgrid_ifft_add", "split_subgrid_fft", "degridder", "layer_fft", "h2d", "d2h", "convert"]
+
+
+class NativeLibraryMissing(RuntimeError):
+    pass
+
+
+class Params(ctypes.Structure):
+    _fields_ = [("vis_count", ctypes.c_int64), ("grid_size", ctypes.c_int32), ("subgrid_size", ctypes.c_int32),
+                ("kernel_size", ctypes.c_int32), ("max_timesteps", ctypes.c_int32), ("scale_arcsec", ctypes.c_float),
+                ("wlayer_count", ctypes.c_int32), ("wstep", ctypes.c_double)]
+
+
+class SubgridC(ctypes.Structure):
+    _fields_ = [("baseline_idx", ctypes.c_int32), ("time_sample_start", ctypes.c_int32),
+                ("time_sample_count", ctypes.c_int32), ("u_pixel", ctypes.c_int32), ("v_pixel", ctypes.c_int32),
+                ("w_lambda", ctypes.c_int32)]
+
+
+class PlanInfo(ctypes.Structure):
+    _fields_ = [("num_subgrids", ctypes.c_int64), ("input_visibilities", ctypes.c_int64),
+                ("gridded_visibilities", ctypes.c_int64), ("work_items", ctypes.c_int64),
+                ("nbl", ctypes.c_int32), ("nt", ctypes.c_int32), ("nch", ctypes.c_int32), ("mode", ctypes.c_int32)]
+
+
+# name -> (restype, argtypes); every symbol include/p9idg.h declares
+P = ctypes.c_void_p
+i32, i64, dbl = ctypes.c_int32, ctypes.c_int64, ctypes.c_double
+SIGNATURES = {
+    "p9idg_plan_create": (i32, [P, P, i32, i32, P, i32, ctypes.POINTER(P)]),
+    "p9idg_plan_create_from_subgrids": (i32, [P, P, i64, P, i32, i32, P, i32, ctypes.POINTER(P)]),
+    "p9idg_plan_num_subgrids": (i32, [P, ctypes.POINTER(i64)]),
+    "p9idg_plan_get_subgrids": (i32, [P, P, i64]),
+    "p9idg_plan_get_info": (i32, [P, ctypes.POINTER(PlanInfo)]),
+    "p9idg_plan_set_mode": (i32, [P, i32]),
+    "p9idg_plan_set_taper": (i32, [P, P]),
+    "p9idg_plan_set_stream": (i32, [P, P]),
+    "p9idg_plan_get_stream": (i32, [P, ctypes.POINTER(P)]),
+    "p9idg_plan_destroy": (None, [P]),
+    "p9idg_grid": (i32, [P, P, P, P]),
+    "p9idg_degrid": (i32, [P, P, P, P]),
+    "p9idg_grid_w": (i32, [P, P, P, P]),
+    "p9idg_degrid_w": (i32, [P, P, P, P]),
+    "p9idg_grid_psf": (i32, [P, P, P, P]),
+    "p9idg_to_image": (i32, [P, P, P, P]),
+    "p9idg_calculate_psf": (i32, [P, P, P, P]),
+    "p9idg_wstack_ifft_float": (i32, [P, i32, i32, i64, P]),
+    "p9idg_fft_forward_float": (i32, [P, i32, dbl, P]),
+    "p9idg_fft_backward_float": (i32, [P, i32, dbl, P]),
+    "p9idg_fft_shift": (i32, [P, i32, i32]),
+    "p9idg_grid_w_device": (i32, [P, P, P]),
+    "p9idg_degrid_w_device": (i32, [P, P, P]),
+    "p9idg_grid_device": (i32, [P, P, P]),
+    "p9idg_degrid_device": (i32, [P, P, P]),
+    "p9idg_wstack_image_device": (i32, [P, P, P, i32]),
+    "p9idg_synchronize": (i32, [P]),
+    "p9idg_plan_enable_timing": (i32, [P, i32]),
+    "p9idg_plan_stage_times": (i32, [P, P, P]),
+    "p9idg_plan_reset_timing": (i32, [P]),
+    "p9idg_last_error": (ctypes.c_char_p, []),
+    "p9idg_version": (ctypes.c_char_p, []),
+    "p9idg_device_count": (i32, []),
+    "p9idg_measure_sincos_peak": (i32, [ctypes.POINTER(dbl), ctypes.POINTER(dbl)]),
+}
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise NativeLibraryMissing(
+                f"{LIB_PATH} is not built; run __graft_entry__.build() (nvcc for sm_103a)")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def last_error() -> str:
+    return lib().p9idg_last_error().decode(errors="replace")

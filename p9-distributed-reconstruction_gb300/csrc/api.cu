@@ -1,0 +1,927 @@
+// C ABI of the GB300 gridder (include/p9idg.h): plans, device buffers, streams, cuFFT
+// plans, stage timing, and the IDG / FFT entry points that replace
+// Distributed-Reconstruction/Core/ImageDomainGridder/IDG.cs and Core/FFT.cs.
+//
+// A plan is created on the host only (partitioning needs no GPU); device state is
+// created on the first call that needs it, on the device current at that time.
+
+#include <cuda_runtime.h>
+#include <cufft.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "kernels.cuh"
+#include "tc_gridder.cuh"
+
+using namespace p9idg;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+p9idg_status fail(p9idg_status st, const std::string &msg) {
+    g_last_error = msg;
+    return st;
+}
+
+p9idg_status cuda_fail(cudaError_t e, const char *what) {
+    const p9idg_status st = (e == cudaErrorMemoryAllocation) ? P9IDG_OUT_OF_MEMORY
+                            : (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) ? P9IDG_NO_DEVICE
+                                                                                             : P9IDG_CUDA_ERROR;
+    return fail(st, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(x)                                                   \
+    do {                                                        \
+        cudaError_t e_ = (x);                                   \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #x);        \
+    } while (0)
+
+#define TRY(x)                                \
+    do {                                      \
+        p9idg_status s_ = (x);                \
+        if (s_ != P9IDG_OK) return s_;        \
+    } while (0)
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+    cudaError_t ensure(size_t n) {
+        if (n <= bytes && p) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+        cudaError_t e = cudaMalloc(&p, std::max<size_t>(n, 256));
+        if (e == cudaSuccess) bytes = std::max<size_t>(n, 256);
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    template <typename T>
+    T *as() const { return static_cast<T *>(p); }
+};
+
+struct FftCache {
+    cufftHandle h = 0;
+    int n = 0;
+    cudaStream_t st = nullptr;
+    p9idg_status get(int size, cudaStream_t stream, cufftHandle *out) {
+        if (h && n != size) {
+            cufftDestroy(h);
+            h = 0;
+        }
+        if (!h) {
+            if (cufftPlan2d(&h, size, size, CUFFT_C2C) != CUFFT_SUCCESS) {
+                h = 0;
+                return fail(P9IDG_CUDA_ERROR, "cufftPlan2d failed");
+            }
+            n = size;
+            st = nullptr;
+        }
+        if (st != stream) {
+            cufftSetStream(h, stream);
+            st = stream;
+        }
+        *out = h;
+        return P9IDG_OK;
+    }
+    void release() {
+        if (h) cufftDestroy(h);
+        h = 0;
+        n = 0;
+    }
+};
+
+struct PendingTiming {
+    int stage;
+    cudaEvent_t a, b;
+};
+
+}  // namespace
+
+struct p9idg_plan {
+    p9idg_params c{};
+    int32_t nbl = 0, nt = 0, nch = 0;
+    int32_t mode = P9IDG_MODE_FP32;
+    std::vector<double> freq, wn, uvw;
+    std::vector<p9idg_subgrid> subs;
+    std::vector<DevSubgrid> dsub;
+    std::vector<WorkItem> gitems, ditems;
+    int32_t nslots = 0;
+    int64_t gridded_vis = 0;
+    std::vector<float> lmn, taper;
+    std::vector<float> add_phasor;  // interleaved float2 [S][S]
+    bool taper_dirty = true;
+
+    // device state
+    bool dev_ready = false;
+    int device = -1;
+    cudaStream_t own_stream = nullptr, stream = nullptr;
+    bool uvw_uploaded = false;
+    DevBuf d_uvw, d_wn, d_sub, d_gitems, d_ditems, d_lmn, d_taper, d_phasor, d_status;
+    DevBuf d_partials, d_subgrids, d_vis_in, d_vis_out, d_layers, d_out128, d_grid128, d_grid128b, d_grid64,
+        d_flags, d_image;
+    TcPlanState tc;
+    FftCache fft;
+
+    bool timing = false;
+    std::vector<PendingTiming> pending;
+    std::vector<cudaEvent_t> event_pool;
+    double stage_ms[P9IDG_NUM_STAGES] = {0};
+    int64_t stage_launches[P9IDG_NUM_STAGES] = {0};
+
+    Geometry geom() const {
+        Geometry g;
+        g.N = c.grid_size;
+        g.S = c.subgrid_size;
+        g.W = c.wlayer_count;
+        g.nch = nch;
+        g.nt_all = nt;
+        g.nbl = nbl;
+        g.uv_scale = 2 * kPi / static_cast<double>(image_size(c));
+        g.wstep_lambda = 0.0f;  // GriddingConstants.WStepLambda is never assigned
+        g.inv_s2 = 1.0f / static_cast<float>(c.subgrid_size * c.subgrid_size);
+        return g;
+    }
+};
+
+namespace {
+
+// ---------- timing ----------
+
+cudaEvent_t take_event(p9idg_plan *p) {
+    if (!p->event_pool.empty()) {
+        cudaEvent_t e = p->event_pool.back();
+        p->event_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+struct StageScope {
+    p9idg_plan *p;
+    int stage;
+    cudaEvent_t a = nullptr;
+    StageScope(p9idg_plan *plan, int s) : p(plan), stage(s) {
+        if (p->timing) {
+            a = take_event(p);
+            cudaEventRecord(a, p->stream);
+        }
+    }
+    ~StageScope() {
+        if (p->timing && a) {
+            cudaEvent_t b = take_event(p);
+            cudaEventRecord(b, p->stream);
+            p->pending.push_back({stage, a, b});
+        }
+    }
+};
+
+void collect_timing(p9idg_plan *p) {
+    for (auto &pt : p->pending) {
+        float ms = 0.f;
+        if (cudaEventSynchronize(pt.b) == cudaSuccess && cudaEventElapsedTime(&ms, pt.a, pt.b) == cudaSuccess) {
+            p->stage_ms[pt.stage] += ms;
+            p->stage_launches[pt.stage] += 1;
+        }
+        p->event_pool.push_back(pt.a);
+        p->event_pool.push_back(pt.b);
+    }
+    p->pending.clear();
+}
+
+// ---------- plan construction ----------
+
+p9idg_status check_params(const p9idg_params *c) {
+    if (!c) return fail(P9IDG_INVALID_ARGUMENT, "null params");
+    if (c->grid_size <= 0 || c->subgrid_size <= 0 || c->subgrid_size > c->grid_size || c->wlayer_count < 0)
+        return fail(P9IDG_INVALID_ARGUMENT, "invalid grid/subgrid/w-layer sizes");
+    return P9IDG_OK;
+}
+
+void finish_plan(p9idg_plan *p) {
+    const int S = p->c.subgrid_size;
+    // Gridder keeps whole time samples per item: up to ~1024 visibilities per item,
+    // degridder up to 512 (4 per thread of a 128-thread block).
+    std::vector<DevSubgrid> tmp;
+    build_work_items(p->subs, p->nch, 1024, p->dsub, p->gitems);
+    build_work_items(p->subs, p->nch, 512, tmp, p->ditems);
+    p->nslots = 0;
+    p->gridded_vis = 0;
+    for (const auto &d : p->dsub) p->nslots += d.item_count;
+    for (const auto &s : p->subs) p->gridded_vis += static_cast<int64_t>(s.time_sample_count) * p->nch;
+    const float img = image_size(p->c);
+    p->lmn.assign(S + S * S, 0.f);
+    for (int x = 0; x < S; x++) p->lmn[x] = compute_l(x, S, img);
+    for (int y = 0; y < S; y++)
+        for (int x = 0; x < S; x++) p->lmn[S + y * S + x] = compute_n(p->lmn[x], p->lmn[y]);
+    p->taper.assign(S * S, 1.0f);  // CalcIdentitySpheroidal (MathFunctions.cs:69-78)
+    p->add_phasor.assign(2 * S * S, 0.f);
+    for (int y = 0; y < S; y++)
+        for (int x = 0; x < S; x++) {
+            const double ph = kPi * static_cast<double>(x + y - S) / static_cast<double>(S);  // Adder.cs:39
+            p->add_phasor[2 * (y * S + x)] = static_cast<float>(std::cos(ph));
+            p->add_phasor[2 * (y * S + x) + 1] = static_cast<float>(std::sin(ph));
+        }
+    p->wn.resize(p->nch);
+    for (int i = 0; i < p->nch; i++) p->wn[i] = wavenumber(p->freq[i]);
+}
+
+// ---------- device state ----------
+
+p9idg_status ensure_device(p9idg_plan *p) {
+    if (p->dev_ready) {
+        CK(cudaSetDevice(p->device));
+        return P9IDG_OK;
+    }
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count == 0) return fail(P9IDG_NO_DEVICE, "no CUDA device available");
+    CK(cudaGetDevice(&p->device));
+    CK(cudaStreamCreateWithFlags(&p->own_stream, cudaStreamNonBlocking));
+    if (!p->stream) p->stream = p->own_stream;
+    const int S = p->c.subgrid_size;
+    CK(p->d_wn.ensure(sizeof(double) * std::max(1, p->nch)));
+    CK(p->d_sub.ensure(sizeof(DevSubgrid) * std::max<size_t>(1, p->dsub.size())));
+    CK(p->d_gitems.ensure(sizeof(WorkItem) * std::max<size_t>(1, p->gitems.size())));
+    CK(p->d_ditems.ensure(sizeof(WorkItem) * std::max<size_t>(1, p->ditems.size())));
+    CK(p->d_lmn.ensure(sizeof(float) * p->lmn.size()));
+    CK(p->d_taper.ensure(sizeof(float) * S * S));
+    CK(p->d_phasor.ensure(sizeof(float) * 2 * S * S));
+    CK(p->d_status.ensure(sizeof(int32_t)));
+    cudaStream_t st = p->stream;
+    CK(cudaMemcpyAsync(p->d_wn.p, p->wn.data(), sizeof(double) * p->nch, cudaMemcpyHostToDevice, st));
+    if (!p->dsub.empty())
+        CK(cudaMemcpyAsync(p->d_sub.p, p->dsub.data(), sizeof(DevSubgrid) * p->dsub.size(), cudaMemcpyHostToDevice, st));
+    if (!p->gitems.empty())
+        CK(cudaMemcpyAsync(p->d_gitems.p, p->gitems.data(), sizeof(WorkItem) * p->gitems.size(),
+                           cudaMemcpyHostToDevice, st));
+    if (!p->ditems.empty())
+        CK(cudaMemcpyAsync(p->d_ditems.p, p->ditems.data(), sizeof(WorkItem) * p->ditems.size(),
+                           cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(p->d_lmn.p, p->lmn.data(), sizeof(float) * p->lmn.size(), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(p->d_phasor.p, p->add_phasor.data(), sizeof(float) * p->add_phasor.size(),
+                       cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(p->d_status.p, 0, sizeof(int32_t), st));
+    CK(cudaStreamSynchronize(st));
+    p->taper_dirty = true;
+    p->dev_ready = true;
+    return P9IDG_OK;
+}
+
+p9idg_status upload_uvw(p9idg_plan *p, const double *uvw) {
+    const size_t bytes = sizeof(double) * 3 * static_cast<size_t>(p->nbl) * p->nt;
+    CK(p->d_uvw.ensure(bytes));
+    if (uvw) {
+        StageScope t(p, P9IDG_STAGE_H2D);
+        CK(cudaMemcpyAsync(p->d_uvw.p, uvw, bytes, cudaMemcpyHostToDevice, p->stream));
+        p->uvw_uploaded = (uvw == p->uvw.data());
+    } else if (!p->uvw_uploaded) {
+        StageScope t(p, P9IDG_STAGE_H2D);
+        CK(cudaMemcpyAsync(p->d_uvw.p, p->uvw.data(), bytes, cudaMemcpyHostToDevice, p->stream));
+        p->uvw_uploaded = true;
+    }
+    return P9IDG_OK;
+}
+
+p9idg_status prepare(p9idg_plan *p, const double *uvw) {
+    TRY(ensure_device(p));
+    if (p->taper_dirty) {
+        CK(cudaMemcpyAsync(p->d_taper.p, p->taper.data(), sizeof(float) * p->taper.size(), cudaMemcpyHostToDevice,
+                           p->stream));
+        p->taper_dirty = false;
+    }
+    CK(cudaMemsetAsync(p->d_status.p, 0, sizeof(int32_t), p->stream));
+    return upload_uvw(p, uvw);
+}
+
+p9idg_status finish_call(p9idg_plan *p) {
+    int32_t status = 0;
+    CK(cudaMemcpyAsync(&status, p->d_status.p, sizeof(int32_t), cudaMemcpyDeviceToHost, p->stream));
+    CK(cudaStreamSynchronize(p->stream));
+    if (p->timing) collect_timing(p);
+    if (status != 0)
+        return fail(P9IDG_DEVICE_CHECK_FAILED, "a kernel bounds check tripped (status " + std::to_string(status) + ")");
+    return P9IDG_OK;
+}
+
+GridderArgs gridder_args(p9idg_plan *p) {
+    GridderArgs a{};
+    a.g = p->geom();
+    a.subs = p->d_sub.as<DevSubgrid>();
+    a.uvw = p->d_uvw.as<double>();
+    a.wavenumbers = p->d_wn.as<double>();
+    a.lmn = p->d_lmn.as<float>();
+    a.taper = p->d_taper.as<float>();
+    return a;
+}
+
+SubgridOpArgs subgrid_args(p9idg_plan *p) {
+    SubgridOpArgs a{};
+    a.g = p->geom();
+    a.subs = p->d_sub.as<DevSubgrid>();
+    a.nsub = static_cast<int32_t>(p->dsub.size());
+    a.add_phasor = p->d_phasor.as<float2>();
+    a.status = p->d_status.as<int32_t>();
+    return a;
+}
+
+bool use_tc(const p9idg_plan *p) { return p->mode != P9IDG_MODE_FP32; }
+
+// Adder.Add throws "invalid grid" for subgrids outside [0, N-S) (Adder.cs:30-50).
+p9idg_status check_adder_range(const p9idg_plan *p) {
+    const int N = p->c.grid_size, S = p->c.subgrid_size;
+    for (const auto &s : p->subs)
+        if (!(s.u_pixel >= 0 && s.u_pixel < N - S && s.v_pixel >= 0 && s.v_pixel < N - S))
+            return fail(P9IDG_INVALID_GRID, "invalid grid");
+    return P9IDG_OK;
+}
+
+// AdderWStack.Add indexes grid[subgridW] after its range check (AdderWStack.cs:47-67).
+p9idg_status check_wstack_layers(const p9idg_plan *p) {
+    const int N = p->c.grid_size, S = p->c.subgrid_size, W = p->c.wlayer_count;
+    for (const auto &s : p->subs) {
+        int sx = s.u_pixel, sy = s.v_pixel, sw = s.w_lambda;
+        if (sw < 0) {
+            sx = N - sx - S + 1;
+            sy = N - sy - S + 1;
+            sw = -sw - 1;
+        }
+        if (!(sx >= 1 && sx < N - S && sy >= 1 && sy < N - S)) continue;
+        if (sw >= W) return fail(P9IDG_INVALID_ARGUMENT, "subgrid w layer index outside the w stack");
+    }
+    return P9IDG_OK;
+}
+
+// vis (device, complex64 or complex128) -> layers (device complex64, W or 1 grids)
+p9idg_status run_grid(p9idg_plan *p, const void *d_vis, bool vis_c128, float2 *d_layers, bool wstack) {
+    const int N = p->c.grid_size, S = p->c.subgrid_size;
+    const int nl = wstack ? p->c.wlayer_count : 1;
+    CK(p->d_partials.ensure(sizeof(float2) * S * S * std::max<size_t>(1, p->nslots)));
+    {
+        StageScope t(p, P9IDG_STAGE_GRIDDER);
+        GridderArgs a = gridder_args(p);
+        a.items = p->d_gitems.as<WorkItem>();
+        a.nitems = static_cast<int32_t>(p->gitems.size());
+        a.vis = d_vis;
+        a.vis_c128 = vis_c128;
+        a.partials = p->d_partials.as<float2>();
+        if (use_tc(p)) {
+            TRY(tc_grid(p->tc, a, p->mode, p->stream, g_last_error));
+        } else {
+            CK(launch_gridder_fp32(a, p->stream));
+        }
+    }
+    {
+        StageScope t(p, P9IDG_STAGE_SUBGRID_IFFT_ADD);
+        CK(cudaMemsetAsync(d_layers, 0, sizeof(float2) * static_cast<size_t>(nl) * N * N, p->stream));
+        SubgridOpArgs a = subgrid_args(p);
+        a.partials = p->d_partials.as<float2>();
+        a.layers = d_layers;
+        a.out_shifted = true;  // IDG.cs:17,37
+        a.wstack = wstack;
+        CK(launch_subgrid_ifft_add(a, p->stream));
+    }
+    return P9IDG_OK;
+}
+
+// grid (device complex64) -> vis (device, complex64 or complex128); uncovered samples are 0
+p9idg_status run_degrid(p9idg_plan *p, const float2 *d_grid, bool grid_shifted, void *d_vis, bool out_c128,
+                        bool wstack) {
+    const int S = p->c.subgrid_size;
+    CK(p->d_subgrids.ensure(sizeof(float2) * S * S * std::max<size_t>(1, p->dsub.size())));
+    {
+        StageScope t(p, P9IDG_STAGE_SPLIT_SUBGRID_FFT);
+        SubgridOpArgs a = subgrid_args(p);
+        a.grid = d_grid;
+        a.grid_shifted = grid_shifted;
+        a.subgrids = p->d_subgrids.as<float2>();
+        a.wstack = wstack;
+        CK(launch_split_subgrid_fft(a, p->stream));
+    }
+    {
+        StageScope t(p, P9IDG_STAGE_DEGRIDDER);
+        const size_t nvis = static_cast<size_t>(p->nbl) * p->nt * p->nch;
+        CK(cudaMemsetAsync(d_vis, 0, nvis * (out_c128 ? sizeof(double2) : sizeof(float2)), p->stream));
+        GridderArgs a = gridder_args(p);
+        a.items = p->d_ditems.as<WorkItem>();
+        a.nitems = static_cast<int32_t>(p->ditems.size());
+        a.subgrids = p->d_subgrids.as<float2>();
+        a.vis_out = d_vis;
+        a.out_c128 = out_c128;
+        if (use_tc(p)) {
+            TRY(tc_degrid(p->tc, a, p->mode, p->stream, g_last_error));
+        } else {
+            CK(launch_degridder_fp32(a, p->stream));
+        }
+    }
+    return P9IDG_OK;
+}
+
+size_t vis_count_of(const p9idg_plan *p) { return static_cast<size_t>(p->nbl) * p->nt * p->nch; }
+size_t nn_of(const p9idg_plan *p) { return static_cast<size_t>(p->c.grid_size) * p->c.grid_size; }
+
+p9idg_status h2d(p9idg_plan *p, void *dst, const void *src, size_t bytes) {
+    StageScope t(p, P9IDG_STAGE_H2D);
+    CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, p->stream));
+    return P9IDG_OK;
+}
+
+p9idg_status d2h(p9idg_plan *p, void *dst, const void *src, size_t bytes) {
+    StageScope t(p, P9IDG_STAGE_D2H);
+    CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, p->stream));
+    return P9IDG_OK;
+}
+
+// device layers complex64 -> host Complex (double) array
+p9idg_status layers_to_host(p9idg_plan *p, const float2 *d_layers, size_t count, double *out) {
+    CK(p->d_out128.ensure(sizeof(double2) * count));
+    {
+        StageScope t(p, P9IDG_STAGE_CONVERT);
+        CK(launch_c64_to_c128(d_layers, static_cast<int64_t>(count), p->d_out128.as<double2>(), p->stream));
+    }
+    return d2h(p, out, p->d_out128.p, sizeof(double2) * count);
+}
+
+p9idg_status host_grid_common(p9idg_plan *p, const double *vis, const double *uvw, double *out, bool wstack) {
+    if (!p || !vis || !out) return fail(P9IDG_INVALID_ARGUMENT, "null argument");
+    TRY(wstack ? check_wstack_layers(p) : check_adder_range(p));
+    TRY(prepare(p, uvw));
+    const size_t nvis = vis_count_of(p), nl = wstack ? p->c.wlayer_count : 1;
+    CK(p->d_vis_in.ensure(sizeof(double2) * std::max<size_t>(1, nvis)));
+    CK(p->d_layers.ensure(sizeof(float2) * nl * nn_of(p)));
+    TRY(h2d(p, p->d_vis_in.p, vis, sizeof(double2) * nvis));
+    TRY(run_grid(p, p->d_vis_in.p, true, p->d_layers.as<float2>(), wstack));
+    TRY(layers_to_host(p, p->d_layers.as<float2>(), nl * nn_of(p), out));
+    return finish_call(p);
+}
+
+p9idg_status host_degrid_common(p9idg_plan *p, double *grid_io, const double *uvw, double *vis_out, bool wstack) {
+    if (!p || !grid_io || !vis_out) return fail(P9IDG_INVALID_ARGUMENT, "null argument");
+    TRY(prepare(p, uvw));
+    const size_t nn = nn_of(p), nvis = vis_count_of(p);
+    CK(p->d_grid128.ensure(sizeof(double2) * nn));
+    CK(p->d_grid128b.ensure(sizeof(double2) * nn));
+    CK(p->d_grid64.ensure(sizeof(float2) * nn));
+    CK(p->d_vis_out.ensure(sizeof(double2) * std::max<size_t>(1, nvis)));
+    TRY(h2d(p, p->d_grid128.p, grid_io, sizeof(double2) * nn));
+    {
+        StageScope t(p, P9IDG_STAGE_CONVERT);
+        CK(launch_shift_convert(p->d_grid128.as<double2>(), p->c.grid_size, p->d_grid64.as<float2>(),
+                                p->d_grid128b.as<double2>(), p->stream));
+    }
+    // FFT.Shift(grid) mutates the caller's array (IDG.cs:24,44)
+    TRY(d2h(p, grid_io, p->d_grid128b.p, sizeof(double2) * nn));
+    TRY(run_degrid(p, p->d_grid64.as<float2>(), true, p->d_vis_out.p, true, wstack));
+    TRY(d2h(p, vis_out, p->d_vis_out.p, sizeof(double2) * nvis));
+    return finish_call(p);
+}
+
+// unit visibilities (IDG.cs:52-66) into a device complex64 buffer
+p9idg_status unit_vis_device(p9idg_plan *p, const uint8_t *flags, float2 **d_vis) {
+    const size_t nvis = vis_count_of(p);
+    CK(p->d_flags.ensure(std::max<size_t>(1, nvis)));
+    CK(p->d_vis_in.ensure(sizeof(double2) * std::max<size_t>(1, nvis)));
+    TRY(h2d(p, p->d_flags.p, flags, nvis));
+    {
+        StageScope t(p, P9IDG_STAGE_CONVERT);
+        CK(launch_unit_vis(p->d_flags.as<uint8_t>(), static_cast<int64_t>(nvis), p->d_vis_in.as<float2>(),
+                           p->stream));
+    }
+    *d_vis = p->d_vis_in.as<float2>();
+    return P9IDG_OK;
+}
+
+// grid (device complex64, in place) -> Re(IFFT)/norm, optionally shifted, into d_image (float or double)
+p9idg_status image_from_grid(p9idg_plan *p, float2 *d_grid, double norm, bool shift, float *outf, double *outd) {
+    StageScope t(p, P9IDG_STAGE_LAYER_FFT);
+    cufftHandle h;
+    TRY(p->fft.get(p->c.grid_size, p->stream, &h));
+    if (cufftExecC2C(h, reinterpret_cast<cufftComplex *>(d_grid), reinterpret_cast<cufftComplex *>(d_grid),
+                     CUFFT_INVERSE) != CUFFT_SUCCESS)
+        return fail(P9IDG_CUDA_ERROR, "cufftExecC2C failed");
+    CK(launch_real_part(d_grid, p->c.grid_size, norm, shift, outf, outd, p->stream));
+    return P9IDG_OK;
+}
+
+// ---------- plan-less FFT helpers (FFT.cs entry points) ----------
+
+struct Standalone {
+    std::mutex mu;
+    bool ready = false;
+    int device = -1;
+    cudaStream_t st = nullptr;
+    DevBuf a, b, c;
+    FftCache fft;
+    p9idg_status init() {
+        int count = 0;
+        if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0)
+            return fail(P9IDG_NO_DEVICE, "no CUDA device available");
+        if (!ready) {
+            CK(cudaGetDevice(&device));
+            CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+            ready = true;
+        }
+        CK(cudaSetDevice(device));
+        return P9IDG_OK;
+    }
+};
+
+Standalone &standalone() {
+    static Standalone s;
+    return s;
+}
+
+}  // namespace
+
+// ====================================================================================
+extern "C" {
+
+p9idg_status p9idg_plan_create(const p9idg_params *c, const double *uvw, int32_t nbl, int32_t nt,
+                               const double *frequencies, int32_t nch, p9idg_plan **out) {
+    if (!out) return fail(P9IDG_INVALID_ARGUMENT, "null output pointer");
+    *out = nullptr;
+    TRY(check_params(c));
+    if (nbl < 0 || nt < 0 || nch < 0) return fail(P9IDG_INVALID_ARGUMENT, "negative dimension");
+    if ((static_cast<int64_t>(nbl) * nt > 0 && !uvw) || (nch > 0 && !frequencies))
+        return fail(P9IDG_INVALID_ARGUMENT, "null uvw or frequencies");
+    auto *p = new (std::nothrow) p9idg_plan();
+    if (!p) return fail(P9IDG_OUT_OF_MEMORY, "plan allocation");
+    p->c = *c;
+    p->nbl = nbl;
+    p->nt = nt;
+    p->nch = nch;
+    std::string err;
+    p9idg_status st = partition(*c, uvw, nbl, nt, frequencies, nch, p->subs, err);
+    if (st != P9IDG_OK) {
+        delete p;
+        return fail(st, err);
+    }
+    p->freq.assign(frequencies, frequencies + nch);
+    p->uvw.assign(uvw, uvw + static_cast<size_t>(nbl) * nt * 3);
+    finish_plan(p);
+    *out = p;
+    return P9IDG_OK;
+}
+
+p9idg_status p9idg_plan_create_from_subgrids(const p9idg_params *c, const p9idg_subgrid *subgrids, int64_t nsub,
+                                             const double *uvw, int32_t nbl, int32_t nt,
+                                             const double *frequencies, int32_t nch, p9idg_plan **out) {
+    if (!out) return fail(P9IDG_INVALID_ARGUMENT, "null output pointer");
+    *out = nullptr;
+    TRY(check_params(c));
+    if (nbl < 0 || nt < 0 || nch < 0 || nsub < 0 || (nsub > 0 && !subgrids))
+        return fail(P9IDG_INVALID_ARGUMENT, "invalid dimensions");
+    if ((static_cast<int64_t>(nbl) * nt > 0 && !uvw) || (nch > 0 && !frequencies))
+        return fail(P9IDG_INVALID_ARGUMENT, "null uvw or frequencies");
+    std::string err;
+    TRY(validate_subgrids(*c, subgrids, nsub, nbl, nt, err) == P9IDG_OK ? P9IDG_OK : fail(P9IDG_INVALID_ARGUMENT, err));
+    auto *p = new (std::nothrow) p9idg_plan();
+    if (!p) return fail(P9IDG_OUT_OF_MEMORY, "plan allocation");
+    p->c = *c;
+    p->nbl = nbl;
+    p->nt = nt;
+    p->nch = nch;
+    p->subs.assign(subgrids, subgrids + nsub);
+    p->freq.assign(frequencies, frequencies + nch);
+    p->uvw.assign(uvw, uvw + static_cast<size_t>(nbl) * nt * 3);
+    finish_plan(p);
+    *out = p;
+    return P9IDG_OK;
+}
+
+p9idg_status p9idg_plan_num_subgrids(const p9idg_plan *plan, int64_t *n) {
+    if (!plan || !n) return fail(P9IDG_INVALID_ARGUMENT, "null argument");
+    *n = static_cast<int64_t>(plan->subs.size());
+    return P9IDG_OK;
+}
+
+p9idg_status p9idg_plan_get_subgrids(const p9idg_plan *plan, p9idg_subgrid *out, int64_t capacity) {
+    if (!plan || (!out && !plan->subs.empty())) return fail(P9IDG_INVALID_ARGUMENT, "null argument");
+    if (capacity < static_cast<int64_t>(plan->subs.size())) return fail(P9IDG_INVALID_ARGUMENT, "capacity too small");
+    if (!plan->subs.empty()) std::memcpy(out, plan->subs.data(), sizeof(p9idg_subgrid) * plan->subs.size());
+    return P9IDG_OK;
+}
+
+p9idg_status p9idg_plan_get_info(const p9idg_plan *plan, p9idg_plan_info *out) {
+    if (!plan || !out) return fail(P9IDG_INVALID_ARGUMENT, "null argument");
+    out->num_subgrids = static_cast<int64_t>(plan->subs.size());
+    out->input_visibilities = static_cast<int64_t>(plan->nbl) * plan->nt * plan->nch;
+    out->gridded_visibilities = plan->gridded_vis;
+    out->work_items = static_cast<int64_t>(plan->gitems.size());
+    out->nbl = plan->nbl;
+    out->nt = plan->nt;
+    out->nch = plan->nch;
+    out->mode = plan->mode;
+    return P9IDG_OK;
+}
+
+p9idg_status p9idg_plan_set_mode(p9idg_plan *plan, int32_t mode) {
+    if (!plan) return fail(P9IDG_INVALID_ARGUMENT, "null plan");
+    if (mode != P9IDG_MODE_FP32 && mode != P9IDG_MODE_TC_BF16X3 && mode != P9IDG_MODE_TC_FP16X3)
+        return fail(P9IDG_INVALID_ARGUMENT, "unknown mode");
+    if (mode == P9IDG_MODE_FP32 && !fp32_subgrid_size_supported(plan->c.subgrid_size))
+        return fail(P9IDG_UNSUPPORTED, "subgrid size not supported by the FP32 kernels");
+    if (mode != P9IDG_MODE_FP32 && !tc_subgrid_size_supported(plan->c.subgrid_size))
+        return fail(P9IDG_UNSUPPORTED, "subgrid size not supported by the tensor-core kernels");
+    plan->mode = mode;
+    return P9IDG_OK;
+}
+
+p9idg_status p9idg_plan_set_taper(p9idg_plan *plan, const float *taper) {
+    if (!plan) return fail(P9IDG_INVALID_ARGUMENT, "null plan");
+    const int S = plan->c.subgrid_size;
+    if (taper)
+        plan->taper.assign(taper, taper + S * S);
+    else
+        plan->taper.assign(S * S, 1.0f);
+    plan->taper_dirty = true;
+    return P9IDG_OK;
+}
+
+p9idg_status p9idg_plan_set_stream(p9idg_plan *plan, void *cuda_stream) {
+    if (!plan) return fail(P9IDG_INVALID_ARGUMENT, "null plan");
+    plan->stream = cuda_stream ? static_cast<cudaStream_t>(cuda_stream) : plan->own_stream;
+    return P9IDG_OK;
+}
+
+p9idg_status p9idg_plan_get_stream(const p9idg_plan *plan, void **cuda_stream) {
+    if (!plan || !cuda_stream) return fail(P9IDG_INVALID_ARGUMENT, "null argument");
+    *cuda_stream = plan->stream;
+    return P9IDG_OK;
+}
+
+void p9idg_plan_destroy(p9idg_plan *plan) {
+    if (!plan) return;
+    if (plan->dev_ready) {
+        cudaSetDevice(plan->device);
+        cudaStreamSynchronize(plan->stream);
+        for (auto &pt : plan->pending) {
+            cudaEventDestroy(pt.a);
+            cudaEventDestroy(pt.b);
+        }
+        for (auto e : plan->event_pool) cudaEventDestroy(e);
+        DevBuf *bufs[] = {&plan->d_uvw, &plan->d_wn, &plan->d_sub, &plan->d_gitems, &plan->d_ditems, &plan->d_lmn,
+                          &plan->d_taper, &plan->d_phasor, &plan->d_status, &plan->d_partials, &plan->d_subgrids,
+                          &plan->d_vis_in, &plan->d_vis_out, &plan->d_layers, &plan->d_out128, &plan->d_grid128,
+                          &plan->d_grid128b, &plan->d_grid64, &plan->d_flags, &plan->d_image};
+        for (DevBuf *b : bufs) b->release();
+        tc_release(plan->tc);
+        plan->fft.release();
+        if (plan->own_stream) cudaStreamDestroy(plan->own_stream);
+    }
+    delete plan;
+}
+
+// ---- IDG facade, host arrays ----
+
+p9idg_status p9idg_grid(p9idg_plan *plan, const double *vis, const double *uvw, double *grid_out) {
+    return host_grid_common(plan, vis, uvw, grid_out, false);
+}
+
+p9idg_status p9idg_grid_w(p9idg_plan *plan, const double *vis, const double *uvw, double *layers_out) {
+    return host_grid_common(plan, vis, uvw, layers_out, true);
+}
+
+p9idg_status p9idg_degrid(p9idg_plan *plan, double *grid_io, const double *uvw, double *vis_out) {
+    return host_degrid_common(plan, grid_io, uvw, vis_out, false);
+}
+
+p9idg_status p9idg_degrid_w(p9idg_plan *plan, double *grid_io, const double *uvw, double *vis_out) {
+    return host_degrid_common(plan, grid_io, uvw, vis_out, true);
+}
+
+p9idg_status p9idg_grid_psf(p9idg_plan *plan, const double *uvw, const uint8_t *flags, double *grid_out) {
+    if (!plan || !flags || !grid_out) return fail(P9IDG_INVALID_ARGUMENT, "null argument");
+    TRY(check_adder_range(plan));
+    TRY(prepare(plan, uvw));
+    float2 *d_vis = nullptr;
+    TRY(unit_vis_device(plan, flags, &d_vis));
+    CK(plan->d_layers.ensure(sizeof(float2) * nn_of(plan)));
+    TRY(run_grid(plan, d_vis, false, plan->d_layers.as<float2>(), false));
+    TRY(layers_to_host(plan, plan->d_layers.as<float2>(), nn_of(plan), grid_out));
+    return finish_call(plan);
+}
+
+static p9idg_status to_image_common(p9idg_plan *plan, const void *d_vis, bool c128, double *image_out) {
+    CK(plan->d_layers.ensure(sizeof(float2) * nn_of(plan)));
+    CK(plan->d_image.ensure(sizeof(double) * nn_of(plan)));
+    TRY(run_grid(plan, d_vis, c128, plan->d_layers.as<float2>(), false));
+    // FFT.Backward(grid, VisibilitiesCount) then FFT.Shift (IDG.cs:74-75)
+    TRY(image_from_grid(plan, plan->d_layers.as<float2>(), static_cast<double>(plan->c.vis_count), true, nullptr,
+                        plan->d_image.as<double>()));
+    TRY(d2h(plan, image_out, plan->d_image.p, sizeof(double) * nn_of(plan)));
+    return finish_call(plan);
+}
+
+p9idg_status p9idg_to_image(p9idg_plan *plan, const double *vis, const double *uvw, double *image_out) {
+    if (!plan || !vis || !image_out) return fail(P9IDG_INVALID_ARGUMENT, "null argument");
+    TRY(check_adder_range(plan));
+    TRY(prepare(plan, uvw));
+    const size_t nvis = vis_count_of(plan);
+    CK(plan->d_vis_in.ensure(sizeof(double2) * std::max<size_t>(1, nvis)));
+    TRY(h2d(plan, plan->d_vis_in.p, vis, sizeof(double2) * nvis));
+    return to_image_common(plan, plan->d_vis_in.p, true, image_out);
+}
+
+p9idg_status p9idg_calculate_psf(p9idg_plan *plan, const double *uvw, const uint8_t *flags, double *psf_out) {
+    if (!plan || !flags || !psf_out) return fail(P9IDG_INVALID_ARGUMENT, "null argument");
+    TRY(check_adder_range(plan));
+    TRY(prepare(plan, uvw));
+    float2 *d_vis = nullptr;
+    TRY(unit_vis_device(plan, flags, &d_vis));
+    return to_image_common(plan, d_vis, false, psf_out);
+}
+
+// ---- FFT.cs ----
+
+p9idg_status p9idg_wstack_ifft_float(const double *layers, int32_t nlayers, int32_t n, int64_t vis_count,
+                                     float *image_out) {
+    if (!image_out || n <= 0 || nlayers < 0 || (nlayers > 0 && !layers))
+        return fail(P9IDG_INVALID_ARGUMENT, "invalid argument");
+    Standalone &s = standalone();
+    std::lock_guard<std::mutex> lk(s.mu);
+    TRY(s.init());
+    const size_t nn = static_cast<size_t>(n) * n;
+    if (nlayers == 0) {
+        std::memset(image_out, 0, sizeof(float) * nn);
+        return P9IDG_OK;
+    }
+    CK(s.a.ensure(sizeof(double2) * nn * nlayers));
+    CK(s.b.ensure(sizeof(float2) * nn));
+    CK(s.c.ensure(sizeof(float) * nn));
+    CK(cudaMemcpyAsync(s.a.p, layers, sizeof(double2) * nn * nlayers, cudaMemcpyHostToDevice, s.st));
+    CK(launch_layer_sum(s.a.p, true, nlayers, static_cast<int64_t>(nn), s.b.as<float2>(), s.st));
+    cufftHandle h;
+    TRY(s.fft.get(n, s.st, &h));
+    if (cufftExecC2C(h, s.b.as<cufftComplex>(), s.b.as<cufftComplex>(), CUFFT_INVERSE) != CUFFT_SUCCESS)
+        return fail(P9IDG_CUDA_ERROR, "cufftExecC2C failed");
+    CK(launch_real_part(s.b.as<float2>(), n, static_cast<double>(vis_count), false, s.c.as<float>(), nullptr, s.st));
+    CK(cudaMemcpyAsync(image_out, s.c.p, sizeof(float) * nn, cudaMemcpyDeviceToHost, s.st));
+    CK(cudaStreamSynchronize(s.st));
+    return P9IDG_OK;
+}
+
+p9idg_status p9idg_fft_forward_float(const float *image, int32_t n, double norm, double *grid_out) {
+    if (!image || !grid_out || n <= 0) return fail(P9IDG_INVALID_ARGUMENT, "invalid argument");
+    Standalone &s = standalone();
+    std::lock_guard<std::mutex> lk(s.mu);
+    TRY(s.init());
+    const size_t nn = static_cast<size_t>(n) * n;
+    CK(s.a.ensure(sizeof(double2) * nn));
+    CK(s.b.ensure(sizeof(float2) * nn));
+    CK(s.c.ensure(sizeof(float) * nn));
+    CK(cudaMemcpyAsync(s.c.p, image, sizeof(float) * nn, cudaMemcpyHostToDevice, s.st));
+    CK(launch_real_to_c64(s.c.as<float>(), static_cast<int64_t>(nn), s.b.as<float2>(), s.st));
+    cufftHandle h;
+    TRY(s.fft.get(n, s.st, &h));
+    if (cufftExecC2C(h, s.b.as<cufftComplex>(), s.b.as<cufftComplex>(), CUFFT_FORWARD) != CUFFT_SUCCESS)
+        return fail(P9IDG_CUDA_ERROR, "cufftExecC2C failed");
+    CK(launch_scale_c64_to_c128(s.b.as<float2>(), static_cast<int64_t>(nn), norm, s.a.as<double2>(), s.st));
+    CK(cudaMemcpyAsync(grid_out, s.a.p, sizeof(double2) * nn, cudaMemcpyDeviceToHost, s.st));
+    CK(cudaStreamSynchronize(s.st));
+    return P9IDG_OK;
+}
+
+p9idg_status p9idg_fft_backward_float(const double *grid, int32_t n, double norm, float *image_out) {
+    if (!grid || !image_out || n <= 0) return fail(P9IDG_INVALID_ARGUMENT, "invalid argument");
+    Standalone &s = standalone();
+    std::lock_guard<std::mutex> lk(s.mu);
+    TRY(s.init());
+    const size_t nn = static_cast<size_t>(n) * n;
+    CK(s.a.ensure(sizeof(double2) * nn));
+    CK(s.b.ensure(sizeof(float2) * nn));
+    CK(s.c.ensure(sizeof(float) * nn));
+    CK(cudaMemcpyAsync(s.a.p, grid, sizeof(double2) * nn, cudaMemcpyHostToDevice, s.st));
+    CK(launch_c128_to_c64(s.a.as<double2>(), static_cast<int64_t>(nn), s.b.as<float2>(), s.st));
+    cufftHandle h;
+    TRY(s.fft.get(n, s.st, &h));
+    if (cufftExecC2C(h, s.b.as<cufftComplex>(), s.b.as<cufftComplex>(), CUFFT_INVERSE) != CUFFT_SUCCESS)
+        return fail(P9IDG_CUDA_ERROR, "cufftExecC2C failed");
+    CK(launch_real_part(s.b.as<float2>(), n, norm, false, s.c.as<float>(), nullptr, s.st));
+    CK(cudaMemcpyAsync(image_out, s.c.p, sizeof(float) * nn, cudaMemcpyDeviceToHost, s.st));
+    CK(cudaStreamSynchronize(s.st));
+    return P9IDG_OK;
+}
+
+p9idg_status p9idg_fft_shift(void *array, int32_t n, int32_t elem_bytes) {
+    if (!array || n < 0 || (elem_bytes != 4 && elem_bytes != 8 && elem_bytes != 16))
+        return fail(P9IDG_INVALID_ARGUMENT, "invalid argument");
+    fft_shift_host(array, n, elem_bytes);
+    return P9IDG_OK;
+}
+
+// ---- device-resident interface ----
+
+p9idg_status p9idg_grid_w_device(p9idg_plan *plan, const void *d_vis, void *d_layers) {
+    if (!plan || !d_vis || !d_layers) return fail(P9IDG_INVALID_ARGUMENT, "null argument");
+    TRY(check_wstack_layers(plan));
+    TRY(prepare(plan, nullptr));
+    return run_grid(plan, d_vis, false, static_cast<float2 *>(d_layers), true);
+}
+
+p9idg_status p9idg_degrid_w_device(p9idg_plan *plan, const void *d_grid, void *d_vis) {
+    if (!plan || !d_grid || !d_vis) return fail(P9IDG_INVALID_ARGUMENT, "null argument");
+    TRY(prepare(plan, nullptr));
+    return run_degrid(plan, static_cast<const float2 *>(d_grid), false, d_vis, false, true);
+}
+
+p9idg_status p9idg_grid_device(p9idg_plan *plan, const void *d_vis, void *d_grid) {
+    if (!plan || !d_vis || !d_grid) return fail(P9IDG_INVALID_ARGUMENT, "null argument");
+    TRY(check_adder_range(plan));
+    TRY(prepare(plan, nullptr));
+    return run_grid(plan, d_vis, false, static_cast<float2 *>(d_grid), false);
+}
+
+p9idg_status p9idg_degrid_device(p9idg_plan *plan, const void *d_grid, void *d_vis) {
+    if (!plan || !d_grid || !d_vis) return fail(P9IDG_INVALID_ARGUMENT, "null argument");
+    TRY(prepare(plan, nullptr));
+    return run_degrid(plan, static_cast<const float2 *>(d_grid), false, d_vis, false, false);
+}
+
+p9idg_status p9idg_wstack_image_device(p9idg_plan *plan, const void *d_layers, float *d_image, int32_t shift) {
+    if (!plan || !d_layers || !d_image) return fail(P9IDG_INVALID_ARGUMENT, "null argument");
+    TRY(ensure_device(plan));
+    CK(plan->d_grid64.ensure(sizeof(float2) * nn_of(plan)));
+    {
+        StageScope t(plan, P9IDG_STAGE_LAYER_FFT);
+        CK(launch_layer_sum(d_layers, false, plan->c.wlayer_count, static_cast<int64_t>(nn_of(plan)),
+                            plan->d_grid64.as<float2>(), plan->stream));
+    }
+    return image_from_grid(plan, plan->d_grid64.as<float2>(), static_cast<double>(plan->c.vis_count), shift != 0,
+                           d_image, nullptr);
+}
+
+p9idg_status p9idg_synchronize(p9idg_plan *plan) {
+    if (!plan) return fail(P9IDG_INVALID_ARGUMENT, "null plan");
+    if (!plan->dev_ready) return P9IDG_OK;
+    CK(cudaSetDevice(plan->device));
+    return finish_call(plan);
+}
+
+// ---- timing ----
+
+p9idg_status p9idg_plan_enable_timing(p9idg_plan *plan, int32_t on) {
+    if (!plan) return fail(P9IDG_INVALID_ARGUMENT, "null plan");
+    plan->timing = on != 0;
+    return P9IDG_OK;
+}
+
+p9idg_status p9idg_plan_stage_times(p9idg_plan *plan, double *ms, int64_t *launches) {
+    if (!plan || !ms) return fail(P9IDG_INVALID_ARGUMENT, "null argument");
+    if (plan->dev_ready) {
+        CK(cudaSetDevice(plan->device));
+        CK(cudaStreamSynchronize(plan->stream));
+        collect_timing(plan);
+    }
+    for (int i = 0; i < P9IDG_NUM_STAGES; i++) {
+        ms[i] = plan->stage_ms[i];
+        if (launches) launches[i] = plan->stage_launches[i];
+    }
+    return P9IDG_OK;
+}
+
+p9idg_status p9idg_plan_reset_timing(p9idg_plan *plan) {
+    if (!plan) return fail(P9IDG_INVALID_ARGUMENT, "null plan");
+    if (plan->dev_ready) {
+        CK(cudaSetDevice(plan->device));
+        CK(cudaStreamSynchronize(plan->stream));
+        collect_timing(plan);
+    }
+    for (int i = 0; i < P9IDG_NUM_STAGES; i++) {
+        plan->stage_ms[i] = 0;
+        plan->stage_launches[i] = 0;
+    }
+    return P9IDG_OK;
+}
+
+// ---- misc ----
+
+const char *p9idg_last_error(void) { return g_last_error.c_str(); }
+
+const char *p9idg_version(void) { return "p9idg-gb300 0.1 (sm_103a)"; }
+
+int32_t p9idg_device_count(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) return 0;
+    return n;
+}
+
+p9idg_status p9idg_measure_sincos_peak(double *sincos_per_s, double *fma_per_s) {
+    if (!sincos_per_s || !fma_per_s) return fail(P9IDG_INVALID_ARGUMENT, "null argument");
+    if (p9idg_device_count() == 0) return fail(P9IDG_NO_DEVICE, "no CUDA device available");
+    CK(measure_sincos(sincos_per_s, fma_per_s));
+    return P9IDG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,248 @@
+// Grid-wide element kernels: FFT.Shift folded into conversions, complex128 <-> complex64
+// boundary conversions, unit (PSF) visibilities, the w-layer sum and the real-part
+// extraction that follows the full-grid inverse FFT (FFT.WStackIFFTFloat, FFT.cs:188-215;
+// FFT.Backward, FFT.cs:159-185), plus the sincos throughput probe used as the FP32/SFU
+// roofline denominator.  All are grid-stride loops sized to the SM count.
+
+#include "kernels.cuh"
+
+namespace p9idg {
+
+namespace {
+
+int grid_blocks(int64_t n, int threads) {
+    static int sms = 0;
+    if (sms == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 132;
+    }
+    const int64_t want = (n + threads - 1) / threads;
+    return static_cast<int>(want < static_cast<int64_t>(sms) * 8 ? (want > 0 ? want : 1) : sms * 8);
+}
+
+__global__ void shift_convert_kernel(const double2 *__restrict__ in, int n, float2 *__restrict__ out64,
+                                     double2 *__restrict__ out128) {
+    const int64_t nn = static_cast<int64_t>(n) * n;
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < nn;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        int r = static_cast<int>(i / n), c = static_cast<int>(i - (i / n) * n);
+        shift_index(n, r, c);
+        const double2 v = in[static_cast<int64_t>(r) * n + c];
+        out64[i] = make_float2(static_cast<float>(v.x), static_cast<float>(v.y));
+        if (out128) out128[i] = v;
+    }
+}
+
+__global__ void c64_to_c128_kernel(const float2 *__restrict__ in, int64_t count, double2 *__restrict__ out) {
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < count;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const float2 v = in[i];
+        out[i] = make_double2(v.x, v.y);
+    }
+}
+
+__global__ void c128_to_c64_kernel(const double2 *__restrict__ in, int64_t count, float2 *__restrict__ out) {
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < count;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const double2 v = in[i];
+        out[i] = make_float2(static_cast<float>(v.x), static_cast<float>(v.y));
+    }
+}
+
+__global__ void unit_vis_kernel(const uint8_t *__restrict__ flags, int64_t count, float2 *__restrict__ out) {
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < count;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+        out[i] = make_float2(flags[i] ? 0.f : 1.f, 0.f);  // IDG.cs:59-62
+}
+
+template <typename T>
+__global__ void layer_sum_kernel(const T *__restrict__ layers, int nlayers, int64_t nn, float2 *__restrict__ out) {
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < nn;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        double re = 0, im = 0;
+        for (int k = 0; k < nlayers; k++) {
+            const T v = layers[static_cast<int64_t>(k) * nn + i];
+            re += v.x;
+            im += v.y;
+        }
+        out[i] = make_float2(static_cast<float>(re), static_cast<float>(im));
+    }
+}
+
+__global__ void real_part_kernel(const float2 *__restrict__ in, int n, double norm, bool shift,
+                                 float *__restrict__ outf, double *__restrict__ outd) {
+    const int64_t nn = static_cast<int64_t>(n) * n;
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < nn;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        int r = static_cast<int>(i / n), c = static_cast<int>(i - (i / n) * n);
+        if (shift) shift_index(n, r, c);
+        const double v = static_cast<double>(in[static_cast<int64_t>(r) * n + c].x) / norm;
+        if (outf) outf[i] = static_cast<float>(v);
+        if (outd) outd[i] = v;
+    }
+}
+
+__global__ void real_to_c64_kernel(const float *__restrict__ in, int64_t count, float2 *__restrict__ out) {
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < count;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+        out[i] = make_float2(in[i], 0.f);
+}
+
+__global__ void scale_c64_to_c128_kernel(const float2 *__restrict__ in, int64_t count, double norm,
+                                         double2 *__restrict__ out) {
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < count;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const float2 v = in[i];
+        out[i] = make_double2(static_cast<double>(v.x) / norm, static_cast<double>(v.y) / norm);
+    }
+}
+
+template <typename T>
+__global__ void shift_inplace_kernel(T *a, int n) {
+    const int n2 = n / 2;
+    const int64_t cnt = static_cast<int64_t>(n2) * n2;
+    for (int64_t k = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; k < cnt;
+         k += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const int i = static_cast<int>(k / n2), j = static_cast<int>(k - (k / n2) * n2);
+        const int64_t a13 = static_cast<int64_t>(i) * n + j, b13 = static_cast<int64_t>(i + n2) * n + j + n2;
+        const int64_t a24 = static_cast<int64_t>(i + n2) * n + j, b24 = static_cast<int64_t>(i) * n + j + n2;
+        T t = a[a13];
+        a[a13] = a[b13];
+        a[b13] = t;
+        t = a[a24];
+        a[a24] = a[b24];
+        a[b24] = t;
+    }
+}
+
+// Throughput probe: independent chains of the FP32 hardware sincos the kernels use.
+constexpr int kProbeChains = 8;
+__global__ void sincos_probe_kernel(int iters, float seed, float *sink) {
+    float x[kProbeChains], acc = 0.f;
+#pragma unroll
+    for (int c = 0; c < kProbeChains; c++) x[c] = seed + 0.001f * (threadIdx.x + c);
+    for (int i = 0; i < iters; i++) {
+#pragma unroll
+        for (int c = 0; c < kProbeChains; c++) {
+            float s, co;
+            __sincosf(x[c], &s, &co);
+            x[c] = fmaf(s, 0.5f, co);
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < kProbeChains; c++) acc += x[c];
+    if (acc == 12345.678f) sink[0] = acc;
+}
+
+__global__ void fma_probe_kernel(int iters, float seed, float *sink) {
+    float x[kProbeChains], acc = 0.f;
+#pragma unroll
+    for (int c = 0; c < kProbeChains; c++) x[c] = seed + 0.001f * (threadIdx.x + c);
+    for (int i = 0; i < iters; i++) {
+#pragma unroll
+        for (int c = 0; c < kProbeChains; c++) x[c] = fmaf(x[c], 0.9999f, 0.0001f);
+    }
+#pragma unroll
+    for (int c = 0; c < kProbeChains; c++) acc += x[c];
+    if (acc == 12345.678f) sink[0] = acc;
+}
+
+}  // namespace
+
+cudaError_t launch_shift_convert(const double2 *in, int n, float2 *out64, double2 *out128, cudaStream_t st) {
+    shift_convert_kernel<<<grid_blocks(static_cast<int64_t>(n) * n, 256), 256, 0, st>>>(in, n, out64, out128);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_c64_to_c128(const float2 *in, int64_t count, double2 *out, cudaStream_t st) {
+    if (count == 0) return cudaSuccess;
+    c64_to_c128_kernel<<<grid_blocks(count, 256), 256, 0, st>>>(in, count, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_c128_to_c64(const double2 *in, int64_t count, float2 *out, cudaStream_t st) {
+    if (count == 0) return cudaSuccess;
+    c128_to_c64_kernel<<<grid_blocks(count, 256), 256, 0, st>>>(in, count, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_unit_vis(const uint8_t *flags, int64_t count, float2 *out, cudaStream_t st) {
+    if (count == 0) return cudaSuccess;
+    unit_vis_kernel<<<grid_blocks(count, 256), 256, 0, st>>>(flags, count, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_layer_sum(const void *layers, bool c128, int nlayers, int64_t nn, float2 *out, cudaStream_t st) {
+    if (c128)
+        layer_sum_kernel<double2><<<grid_blocks(nn, 256), 256, 0, st>>>(static_cast<const double2 *>(layers),
+                                                                         nlayers, nn, out);
+    else
+        layer_sum_kernel<float2><<<grid_blocks(nn, 256), 256, 0, st>>>(static_cast<const float2 *>(layers),
+                                                                        nlayers, nn, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_real_part(const float2 *in, int n, double norm, bool shift, float *outf, double *outd,
+                             cudaStream_t st) {
+    real_part_kernel<<<grid_blocks(static_cast<int64_t>(n) * n, 256), 256, 0, st>>>(in, n, norm, shift, outf, outd);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_real_to_c64(const float *in, int64_t count, float2 *out, cudaStream_t st) {
+    real_to_c64_kernel<<<grid_blocks(count, 256), 256, 0, st>>>(in, count, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_scale_c64_to_c128(const float2 *in, int64_t count, double norm, double2 *out, cudaStream_t st) {
+    scale_c64_to_c128_kernel<<<grid_blocks(count, 256), 256, 0, st>>>(in, count, norm, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_shift_inplace(void *a, int n, int elem_bytes, cudaStream_t st) {
+    const int64_t cnt = static_cast<int64_t>(n / 2) * (n / 2);
+    if (cnt == 0) return cudaSuccess;
+    const int b = grid_blocks(cnt, 256);
+    switch (elem_bytes) {
+        case 4: shift_inplace_kernel<float><<<b, 256, 0, st>>>(static_cast<float *>(a), n); break;
+        case 8: shift_inplace_kernel<double><<<b, 256, 0, st>>>(static_cast<double *>(a), n); break;
+        case 16: shift_inplace_kernel<double2><<<b, 256, 0, st>>>(static_cast<double2 *>(a), n); break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t measure_sincos(double *sincos_per_s, double *fma_per_s) {
+    int dev = 0, sms = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    float *sink = nullptr;
+    if ((e = cudaMalloc(&sink, sizeof(float))) != cudaSuccess) return e;
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    const int blocks = sms * 8, threads = 256, iters = 4096;
+    sincos_probe_kernel<<<blocks, threads>>>(64, 0.1f, sink);  // warm-up
+    cudaEventRecord(a);
+    sincos_probe_kernel<<<blocks, threads>>>(iters, 0.1f, sink);
+    cudaEventRecord(b);
+    cudaEventSynchronize(b);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    *sincos_per_s = static_cast<double>(blocks) * threads * iters * kProbeChains / (ms * 1e-3);
+    fma_probe_kernel<<<blocks, threads>>>(64, 0.1f, sink);
+    cudaEventRecord(a);
+    fma_probe_kernel<<<blocks, threads>>>(iters * 4, 0.1f, sink);
+    cudaEventRecord(b);
+    cudaEventSynchronize(b);
+    cudaEventElapsedTime(&ms, a, b);
+    *fma_per_s = static_cast<double>(blocks) * threads * iters * 4 * kProbeChains / (ms * 1e-3);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaFree(sink);
+    return cudaGetLastError();
+}
+
+}  // namespace p9idg
