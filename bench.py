@@ -42,7 +42,7 @@ def dist_info():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+    """nvidia-smi clocks and throttle reasons sampled every 100 ms during the timed region."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -55,7 +55,7 @@ class ClockSampler:
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
-                                          "-lms", "200", "-i", str(self.gpu)], stdout=subprocess.PIPE,
+                                          "-lms", "100", "-i", str(self.gpu)], stdout=subprocess.PIPE,
                                          stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -126,15 +126,15 @@ def cpu_reference_step(oracle, cd, sample, obs, model_grid):
 def calibrate_cpu_sample(oracle, cd, subs, obs, model_grid, budget_s):
     """A seeded subgrid sample whose CPU grid+degrid takes about budget_s (from a short pilot)."""
     nch = obs.vis.shape[2]
-    pts = []
-    for n in (40000, 160000):  # two pilots: fixed cost (w-layer allocation, shifts) + per-visibility cost
-        sample, nv = pick_sample(subs, nch, n, seed=1)
-        t0 = time.perf_counter()
-        cpu_reference_step(oracle, cd, sample, obs, model_grid)
-        pts.append((nv, time.perf_counter() - t0))
-    (n1, t1), (n2, t2) = pts
-    per_vis = max((t2 - t1) / max(n2 - n1, 1), 1e-9)
-    fixed = max(t1 - per_vis * n1, 0.0)
+    # two pilots: the fixed cost (w-layer allocation and shifts) and the per-visibility cost
+    t0 = time.perf_counter()
+    cpu_reference_step(oracle, cd, subs[:0], obs, model_grid)
+    fixed = time.perf_counter() - t0
+    sample, n1 = pick_sample(subs, nch, 250000, seed=1)
+    t0 = time.perf_counter()
+    cpu_reference_step(oracle, cd, sample, obs, model_grid)
+    t1 = time.perf_counter() - t0
+    per_vis = max((t1 - fixed) / max(n1, 1), 1e-9)
     target = int(max(budget_s - fixed, 0.5 * budget_s) / per_vis)
     sample, nv = pick_sample(subs, nch, target)
     return sample, nv, fixed
@@ -186,12 +186,14 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--mode", default="auto", choices=["auto"] + list(MODES))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--antennas", type=int, default=None,
+                    help="smaller array (fewer baselines) of the same workload, for profiling captures")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -206,7 +208,7 @@ def main():
     pkg = entry.load_package()
     synth = entry._load_module(entry.PKG_NAME + ".synth", os.path.join(entry.PKG_DIR, "synth.py"))
 
-    wl = synth.scaled_workload(WORKLOAD, seed=synth.WORKLOADS[WORKLOAD]["obs"]["seed"] + rank)
+    wl = synth.scaled_workload(WORKLOAD, n_ant=args.antennas, seed=synth.WORKLOADS[WORKLOAD]["obs"]["seed"] + rank)
     obs, cd = synth.build(wl)
     c = pkg.GriddingConstants.from_dict(cd)
     part = pkg.Partitioner.CreatePartition(c, obs.uvw, obs.frequencies)
