@@ -167,6 +167,23 @@ p9idg_status p9idg_degrid_device(p9idg_plan *plan, const void *d_grid, void *d_v
 p9idg_status p9idg_wstack_image_device(p9idg_plan *plan, const void *d_layers, float *d_image, int32_t shift);
 p9idg_status p9idg_synchronize(p9idg_plan *plan);
 
+/* No counterpart in the reference.  W-stacked gridding (the work of p9idg_grid_w_device, FP32
+ * kernels) for callers that cannot allocate device memory: a pipeline that reserves all of its
+ * memory up front and forbids allocation afterwards, a framework whose allocator owns every
+ * device byte, or a process under a hard device-memory quota.  It takes no plan and calls no
+ * allocator; its working memory is one fixed 32 MiB array in the library's device image, which
+ * every GPU that loads the library holds until the process exits.
+ *   d_subgrids  device array of nsub subgrids (e.g. p9idg_plan_get_subgrids copied to the GPU)
+ *   d_uvw       device double[nbl][nt][3];  frequencies: host double[nch], nch <= 64
+ *   d_vis       device complex64[nbl][nt][nch];  d_layers: device complex64[W][N][N], overwritten
+ * Subgrid sizes 8, 16, 24, 32, 48 only.  Synchronous: returns after the GPU work on cuda_stream
+ * (NULL = legacy default stream) has finished.  The first call on a device looks up the array's
+ * address; make it before any stream capture.  All calls share the array: calls whose GPU work
+ * overlaps race and must be ordered by the caller. */
+p9idg_status p9idg_grid_w_device_noalloc(const p9idg_params *c, const p9idg_subgrid *d_subgrids, int64_t nsub,
+                                         const double *d_uvw, int32_t nbl, int32_t nt, const double *frequencies,
+                                         int32_t nch, const void *d_vis, void *d_layers, void *cuda_stream);
+
 /* ---------------- stage timing (CUDA events on the plan's stream) ---------------- */
 
 enum {

@@ -82,6 +82,7 @@ SIGNATURES = {
     "p9idg_degrid_device": (i32, [P, P, P]),
     "p9idg_wstack_image_device": (i32, [P, P, P, i32]),
     "p9idg_synchronize": (i32, [P]),
+    "p9idg_grid_w_device_noalloc": (i32, [P, P, i64, P, i32, i32, P, i32, P, P, P]),
     "p9idg_plan_enable_timing": (i32, [P, i32]),
     "p9idg_plan_stage_times": (i32, [P, P, P]),
     "p9idg_plan_reset_timing": (i32, [P]),

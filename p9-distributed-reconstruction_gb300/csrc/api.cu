@@ -107,6 +107,8 @@ struct PendingTiming {
 
 }  // namespace
 
+void p9idg::record_last_error(const std::string &msg) { g_last_error = msg; }
+
 struct p9idg_plan {
     p9idg_params c{};
     int32_t nbl = 0, nt = 0, nch = 0;

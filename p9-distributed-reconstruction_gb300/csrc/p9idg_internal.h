@@ -51,4 +51,7 @@ void build_work_items(const std::vector<p9idg_subgrid> &subs, int32_t nch, int64
                       std::vector<DevSubgrid> &dsub, std::vector<WorkItem> &items);
 void fft_shift_host(void *a, int32_t n, int32_t elem_bytes);
 
+// Sets the thread-local message p9idg_last_error() returns (api.cu).
+void record_last_error(const std::string &msg);
+
 }  // namespace p9idg
