@@ -212,6 +212,10 @@ int32_t p9idg_device_count(void);
 /* Measured FP32 sincos throughput of the current device (sincos per second) from a short
  * on-device loop of the intrinsic the FP32 kernels use; the FP32/SFU roofline denominator. */
 p9idg_status p9idg_measure_sincos_peak(double *sincos_per_s, double *fma_per_s);
+/* Runs a known 128 x n x 64 GEMM (n = 32, 64 or 128) through the tensor-core operand layout,
+ * descriptors and TMEM path the P9IDG_MODE_TC_* kernels use; *max_rel_err is the largest error
+ * relative to max |C| (inputs are exactly representable, so it is at FP32-accumulation level). */
+p9idg_status p9idg_tc_selftest(int32_t mode, int32_t n, double *max_rel_err);
 
 #ifdef __cplusplus
 }

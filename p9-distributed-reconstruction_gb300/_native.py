@@ -90,6 +90,7 @@ SIGNATURES = {
     "p9idg_version": (ctypes.c_char_p, []),
     "p9idg_device_count": (i32, []),
     "p9idg_measure_sincos_peak": (i32, [ctypes.POINTER(dbl), ctypes.POINTER(dbl)]),
+    "p9idg_tc_selftest": (i32, [i32, i32, ctypes.POINTER(dbl)]),
 }
 
 _lib = None

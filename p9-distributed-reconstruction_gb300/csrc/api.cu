@@ -325,7 +325,15 @@ GridderArgs gridder_args(p9idg_plan *p) {
     a.wavenumbers = p->d_wn.as<double>();
     a.lmn = p->d_lmn.as<float>();
     a.taper = p->d_taper.as<float>();
+    a.nsub = static_cast<int32_t>(p->dsub.size());
+    a.status = p->d_status.as<int32_t>();
     return a;
+}
+
+p9idg_status ensure_tc(p9idg_plan *p) {
+    if (p->tc.ready) return P9IDG_OK;
+    return tc_prepare(p->tc, p->subs, p->lmn, p->c.subgrid_size, p->nch, p->wn, p->uvw.data(), p->nt, p->stream,
+                      g_last_error);
 }
 
 SubgridOpArgs subgrid_args(p9idg_plan *p) {
@@ -379,6 +387,7 @@ p9idg_status run_grid(p9idg_plan *p, const void *d_vis, bool vis_c128, float2 *d
         a.vis_c128 = vis_c128;
         a.partials = p->d_partials.as<float2>();
         if (use_tc(p)) {
+            TRY(ensure_tc(p));
             TRY(tc_grid(p->tc, a, p->mode, p->stream, g_last_error));
         } else {
             CK(launch_gridder_fp32(a, p->stream));
@@ -422,6 +431,7 @@ p9idg_status run_degrid(p9idg_plan *p, const float2 *d_grid, bool grid_shifted, 
         a.vis_out = d_vis;
         a.out_c128 = out_c128;
         if (use_tc(p)) {
+            TRY(ensure_tc(p));
             TRY(tc_degrid(p->tc, a, p->mode, p->stream, g_last_error));
         } else {
             CK(launch_degridder_fp32(a, p->stream));
@@ -917,6 +927,13 @@ int32_t p9idg_device_count(void) {
     int n = 0;
     if (cudaGetDeviceCount(&n) != cudaSuccess) return 0;
     return n;
+}
+
+p9idg_status p9idg_tc_selftest(int32_t mode, int32_t n, double *max_rel_err) {
+    if (!max_rel_err || (mode != P9IDG_MODE_TC_BF16X3 && mode != P9IDG_MODE_TC_FP16X3))
+        return fail(P9IDG_INVALID_ARGUMENT, "invalid argument");
+    if (p9idg_device_count() == 0) return fail(P9IDG_NO_DEVICE, "no CUDA device available");
+    return tc_selftest(mode, n, max_rel_err, g_last_error);
 }
 
 p9idg_status p9idg_measure_sincos_peak(double *sincos_per_s, double *fma_per_s) {

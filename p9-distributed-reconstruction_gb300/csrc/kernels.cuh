@@ -48,6 +48,8 @@ struct GridderArgs {
     const float2 *subgrids;    // degridder: [nsub][S][S] after SubgridFFT.Backward
     void *vis_out;             // degridder output (complex64 or complex128)
     bool out_c128;
+    int32_t nsub;              // subgrids in `subs`
+    int32_t *status;           // device status word
 };
 
 cudaError_t launch_gridder_fp32(const GridderArgs &a, cudaStream_t st);

@@ -1,25 +1,904 @@
-// Tensor-core gridder/degridder (tcgen05).  Not yet available: every call reports
-// P9IDG_UNSUPPORTED and p9idg_plan_set_mode refuses the tensor-core modes.
+// Tensor-core (tcgen05) gridder and degridder for S = 32, split precision.
+//
+// The per-subgrid phase of the reference (Gridder.cs:61-67, 143-145) is
+//     phi_k(x, y) = du_k l_x + dv_k m_y + dw_k n(x, y)
+// with n the reference's FP32 ComputeN table.  Writing n = f(x) + g(y) + r(x, y), with
+// f(x) = n(l_x, 0), g(y) = n(0, m_y) (the same table) and r the small remainder
+// (~ -l^2 m^2), the phasor factorises as A_k(x) B_k(y) exp(i dw_k r(x, y)) with
+// A_k(x) = exp(i(du_k l_x + dw_k f_x)), B_k(y) = exp(i(dv_k m_y + dw_k g_y)).  To first
+// order in dw r (|dw r| <= ~1e-3 here, second order ~5e-7):
+//   gridder:   P[y][x] = sum_k vis_k A B (1 + i dw_k r) = P0 + i r (.) P1,
+//              P0 = B diag(vis) A^T,  P1 = B diag(vis dw) A^T          (rank-K updates)
+//   degridder: vis_k = 1/S^2 sum_y conj(B_k(y)) [T0_k(y) - i dw_k T1_k(y)],
+//              T_j = sum_x Q_j[y][x] conj(A_k(x)),  Q0 = pix, Q1 = r (.) pix   (GEMM, M = visibilities)
+// Only 2*S sincos per visibility remain (vs S^2 in the FP32 kernels); the contractions
+// run on tcgen05 with BF16 (or FP16) hi+lo operands: x ~ hi + lo, products hi*hi + hi*lo +
+// lo*hi accumulated in FP32 in tensor memory.  The P1 / T1 corrections use hi*hi only.
+//
+// Gridder MMA layout (per 8 visibilities = K16, real form, k = 2 v + re/im):
+//   A rows (192 = 3 blocks of 64, rows p*32 + y):  [A0_lo ; A0_hi ; A1_hi]
+//       p = re: [B_re, -B_im],  p = im: [B_im, B_re];  A1 = dw * A0
+//   B rows (64 = [B_lo ; B_hi], row x): [W_re, W_im] with W = vis * A_k(x)
+//   MMA2: A rows 64-191 x B rows 0-63 (M128 N64) -> TMEM cols 0..63
+//   MMA1: A rows 0-127  x B rows 32-63 (M128 N32) -> TMEM cols 0..31
+//   => P0 = D[lanes 0-63][0:32] + D[lanes 0-63][32:64],  P1 = D[lanes 64-127][32:64]
+// Degridder (per tile of 128 visibilities = rows; k = 2x + re/im):
+//   A rows: [cos, sin](phase_A);  static B rows (192, row 2y+p):  [B0_lo ; B0_hi ; B1_hi]
+//   MMA1: A_hi x B rows 64-191 (N128) -> cols 0..127 = [T0 | T1];  MMA2: A_hi x B0_lo (N64),
+//   MMA3: A_lo x B0_hi (N64) -> cols 0..63.  Two accumulators alternate (256 columns).
+
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
 #include "tc_gridder.cuh"
+#include "tc_ptx.cuh"
 
 namespace p9idg {
 
-bool tc_subgrid_size_supported(int) { return false; }
+namespace {
 
-p9idg_status tc_grid(TcPlanState &, const GridderArgs &, int, cudaStream_t, std::string &err) {
-    err = "tensor-core gridder not available";
-    return P9IDG_UNSUPPORTED;
+using namespace tc;
+
+constexpr int kS = 32;
+constexpr uint64_t kWaitNs = 2000000000ull;  // 2 s per wait before a kernel gives up
+
+// ---------------- bf16 / fp16 splitting ----------------
+
+template <bool BF16>
+struct Half16;
+
+template <>
+struct Half16<true> {
+    static __device__ __forceinline__ uint32_t pack(float a, float b) {
+        __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+        return *reinterpret_cast<uint32_t *>(&h);
+    }
+    static __device__ __forceinline__ float lo_of(uint32_t w) { return __uint_as_float(w << 16); }
+    static __device__ __forceinline__ float hi_of(uint32_t w) { return __uint_as_float(w & 0xFFFF0000u); }
+};
+
+template <>
+struct Half16<false> {
+    static __device__ __forceinline__ uint32_t pack(float a, float b) {
+        __half2 h = __floats2half2_rn(a, b);
+        return *reinterpret_cast<uint32_t *>(&h);
+    }
+    static __device__ __forceinline__ float lo_of(uint32_t w) {
+        return __half2float(__ushort_as_half(static_cast<unsigned short>(w & 0xFFFFu)));
+    }
+    static __device__ __forceinline__ float hi_of(uint32_t w) {
+        return __half2float(__ushort_as_half(static_cast<unsigned short>(w >> 16)));
+    }
+};
+
+// (a, b) -> packed hi pair and packed lo pair (residuals)
+template <bool BF16>
+__device__ __forceinline__ void split_pair(float a, float b, uint32_t &hi, uint32_t &lo) {
+    hi = Half16<BF16>::pack(a, b);
+    lo = Half16<BF16>::pack(a - Half16<BF16>::lo_of(hi), b - Half16<BF16>::hi_of(hi));
 }
 
-p9idg_status tc_degrid(TcPlanState &, const GridderArgs &, int, cudaStream_t, std::string &err) {
-    err = "tensor-core degridder not available";
-    return P9IDG_UNSUPPORTED;
+__device__ __forceinline__ uint32_t neg_hi(uint32_t w) { return w ^ 0x80000000u; }
+__device__ __forceinline__ uint32_t swap_halves(uint32_t w) { return (w >> 16) | (w << 16); }
+
+__device__ __forceinline__ void st_shared_v4(uint32_t addr, uint32_t a, uint32_t b, uint32_t c, uint32_t d) {
+    asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(a), "r"(b), "r"(c), "r"(d)
+                 : "memory");
+}
+
+__device__ __forceinline__ void named_bar(int id, int nthreads) {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
+
+// byte offset of the 16-byte chunk (row, k group) in a K=64 canonical operand tile
+__device__ __forceinline__ uint32_t chunk_off(int row, int kg) {
+    return static_cast<uint32_t>((row >> 3) * 1024 + kg * 128 + (row & 7) * 16);
+}
+
+struct TcArgs {
+    Geometry g;
+    const WorkItem *items;
+    const DevSubgrid *subs;
+    const int64_t *coef_off;
+    const float4 *coef;
+    const void *vis;
+    const float *lmn;   // l[S], n[S*S]
+    const float *tabs;  // f[S], r[S*S]
+    const float *taper;
+    float2 *partials;
+    const float2 *subgrids;
+    void *vis_out;
+    int32_t *status;
+    float dw_scale;  // FP16 operands: power of two bringing max |dw| below 1 (1 for BF16)
+    float r_scale;   // FP16 operands: power of two bringing max |r| below 1 (1 for BF16)
+};
+
+// 2^-e with m * 2^-e in [0.5, 1) (1 for m == 0): exact power-of-two scale
+__device__ __forceinline__ float pow2_scale(float m) {
+    if (!(m > 0.f) || isinf(m)) return 1.f;
+    int e;
+    frexpf(m, &e);
+    return ldexpf(1.f, -e);
+}
+
+// max over the 256 threads of warps 0-7 (named barrier 2); red: 9 floats of shared memory
+__device__ __forceinline__ float block256_max(float v, float *red) {
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    named_bar(2, 256);
+    if (threadIdx.x == 0) {
+        float m = red[0];
+        for (int i = 1; i < 8; i++) m = fmaxf(m, red[i]);
+        red[8] = m;
+    }
+    named_bar(2, 256);
+    return red[8];
+}
+
+// ---------------- per-visibility coefficients (FP64 -> FP32) ----------------
+
+__global__ void tc_coef_kernel(const DevSubgrid *subs, const int64_t *coef_off, const double *uvw, const double *wn,
+                               Geometry g, float4 *coef) {
+    const DevSubgrid sg = subs[blockIdx.x];
+    const double uoff = static_cast<double>(sg.u + g.S / 2 - g.N / 2) * g.uv_scale;
+    const double voff = static_cast<double>(sg.v + g.S / 2 - g.N / 2) * g.uv_scale;
+    const double woff = 2 * kPi * (static_cast<double>(g.wstep_lambda) * (static_cast<double>(sg.w) + 0.5));
+    const int nvis = sg.nt * g.nch;
+    float4 *out = coef + coef_off[blockIdx.x];
+    for (int j = threadIdx.x; j < nvis; j += blockDim.x) {
+        const int t = sg.t0 + j / g.nch, ch = j - (j / g.nch) * g.nch;
+        const double *q = uvw + (static_cast<int64_t>(sg.bl) * g.nt_all + t) * 3;
+        const double k = wn[ch];
+        out[j] = make_float4(static_cast<float>(uoff - k * q[0]), static_cast<float>(voff - k * q[1]),
+                             static_cast<float>(woff - k * q[2]), 0.f);
+    }
+}
+
+// ---------------- gridder ----------------
+
+constexpr int kGVps = 32;      // visibilities per pipeline stage (K = 64)
+constexpr int kGStages = 3;
+constexpr int kGProducerWarps = 8;
+constexpr int kGThreads = (kGProducerWarps + 1) * 32;
+constexpr uint32_t kGStageA = 192 * 64 * 2;
+constexpr uint32_t kGStageB = 64 * 64 * 2;
+constexpr uint32_t kGStageBytes = kGStageA + kGStageB;
+constexpr uint32_t kGSmem = kGStages * kGStageBytes + 256 + 1024;  // + barriers + alignment slack
+constexpr uint32_t kGTmemCols = 64;
+
+template <bool BF16, typename VisT>
+__global__ void __launch_bounds__(kGThreads, 2) tc_gridder_kernel(const TcArgs a) {
+    extern __shared__ unsigned char smem_raw[];
+    unsigned char *smem = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem + kGStages * kGStageBytes);
+    uint64_t *empty = full + kGStages;
+    uint64_t *accb = empty + kGStages;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(accb + 1);
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const Geometry &g = a.g;
+    const WorkItem it = a.items[blockIdx.x];
+    const DevSubgrid sg = a.subs[it.subgrid];
+    const int nvis = it.nt * g.nch;
+    const int nstages = (nvis + kGVps - 1) / kGVps;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kGStages; s++) {
+            mbar_init(&full[s], kGProducerWarps);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(accb, 1);
+        *abort_flag = 0;
+        mbar_fence_init();
+    }
+    if (warp == kGProducerWarps) {
+        tmem_alloc(tmem_slot, kGTmemCols);
+        tmem_relinquish();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+    const uint32_t sbase = smem_u32(smem);
+
+    if (warp == kGProducerWarps) {
+        // ---- MMA issuer ----
+        if (lane == 0) {
+            constexpr uint32_t id32 = idesc_f16(128, 32, BF16), id64 = idesc_f16(128, 64, BF16);
+            for (int i = 0; i < nstages; i++) {
+                const int s = i % kGStages;
+                const uint32_t ph = (i / kGStages) & 1;
+                if (!mbar_wait(&full[s], ph, abort_flag, kWaitNs)) {
+                    *abort_flag = 1;
+                    atomicOr(a.status, kStatusWait);
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t A = sbase + s * kGStageBytes, B = A + kGStageA;
+#pragma unroll
+                for (int kc = 0; kc < 4; kc++) {
+                    mma_f16(tmem, smem_desc(A + 8 * 1024 + kc * 256, 128, 1024), smem_desc(B + kc * 256, 128, 1024),
+                            id64, (i > 0 || kc > 0) ? 1u : 0u);
+                    mma_f16(tmem, smem_desc(A + kc * 256, 128, 1024), smem_desc(B + 4 * 1024 + kc * 256, 128, 1024),
+                            id32, 1u);
+                }
+                mma_commit(&empty[s]);
+            }
+            mma_commit(accb);
+            // the MMAs must be finished before the TMEM is released
+            if (!mbar_wait(accb, 0, abort_flag, kWaitNs)) atomicOr(a.status, kStatusWait);
+        }
+        __syncwarp();
+    } else {
+        // ---- producers: 8 warps; warp = group of 4 visibilities (k group), lane = y (A side) and x (B side)
+        const int group = warp;
+        const float m_y = a.lmn[lane], g_y = a.tabs[lane];  // y-side tables (l and m coincide, f and g coincide)
+        const float l_x = m_y, f_x = g_y;
+        const VisT *vis = static_cast<const VisT *>(a.vis);
+        const int64_t cbase = a.coef_off[it.subgrid] + static_cast<int64_t>(it.t0 - sg.t0) * g.nch;
+        float *red = reinterpret_cast<float *>(tmem_slot + 2);
+        float sv = 1.f;  // FP16: power-of-two scale of this item's visibilities
+        if (!BF16) {
+            float mx = 0.f;
+            for (int j = threadIdx.x; j < nvis; j += kGProducerWarps * 32) {
+                const int t = it.t0 + j / g.nch, ch = j - (j / g.nch) * g.nch;
+                const float2 v = load_vis(vis, (static_cast<int64_t>(sg.bl) * g.nt_all + t) * g.nch + ch);
+                mx = fmaxf(mx, fmaxf(fabsf(v.x), fabsf(v.y)));
+            }
+            sv = pow2_scale(block256_max(mx, red));
+        }
+        const float sw = BF16 ? 1.f : a.dw_scale;
+        for (int i = 0; i < nstages; i++) {
+            const int s = i % kGStages;
+            const uint32_t ph = (i / kGStages) & 1;
+            if (!warp_wait(&empty[s], ph ^ 1, abort_flag, kWaitNs)) {
+                if (lane == 0) {
+                    *abort_flag = 1;
+                    atomicOr(a.status, kStatusWait);
+                }
+                break;
+            }
+            uint32_t alo_re[4], alo_im[4], ahi_re[4], ahi_im[4], a1_re[4], a1_im[4], bhi[4], blo[4];
+#pragma unroll
+            for (int v = 0; v < 4; v++) {
+                const int j = i * kGVps + group * 4 + v;
+                float4 c = make_float4(0.f, 0.f, 0.f, 0.f);
+                float2 vv = make_float2(0.f, 0.f);
+                if (j < nvis) {
+                    c = a.coef[cbase + j];
+                    const int t = it.t0 + j / g.nch, ch = j - (j / g.nch) * g.nch;
+                    vv = load_vis(vis, (static_cast<int64_t>(sg.bl) * g.nt_all + t) * g.nch + ch);
+                }
+                // y side: B_k(y)
+                float sb, cb;
+                __sincosf(fmaf(c.y, m_y, c.z * g_y), &sb, &cb);
+                uint32_t hi, lo;
+                split_pair<BF16>(cb, sb, hi, lo);  // hi = (hre, him), lo = (lre, lim)
+                ahi_re[v] = neg_hi(hi);                 // (hre, -him)
+                ahi_im[v] = swap_halves(hi);            // (him, hre)
+                alo_re[v] = neg_hi(lo);
+                alo_im[v] = swap_halves(lo);
+                const float dws = c.z * sw;
+                const uint32_t h1 = Half16<BF16>::pack(dws * cb, dws * sb);
+                a1_re[v] = neg_hi(h1);
+                a1_im[v] = swap_halves(h1);
+                // x side: W = vis * A_k(x)
+                float sa, ca;
+                __sincosf(fmaf(c.x, l_x, c.z * f_x), &sa, &ca);
+                const float wre = (vv.x * ca - vv.y * sa) * sv, wim = (vv.x * sa + vv.y * ca) * sv;
+                split_pair<BF16>(wre, wim, bhi[v], blo[v]);
+            }
+            const uint32_t A = sbase + s * kGStageBytes, B = A + kGStageA;
+            st_shared_v4(A + chunk_off(lane, group), alo_re[0], alo_re[1], alo_re[2], alo_re[3]);
+            st_shared_v4(A + chunk_off(32 + lane, group), alo_im[0], alo_im[1], alo_im[2], alo_im[3]);
+            st_shared_v4(A + chunk_off(64 + lane, group), ahi_re[0], ahi_re[1], ahi_re[2], ahi_re[3]);
+            st_shared_v4(A + chunk_off(96 + lane, group), ahi_im[0], ahi_im[1], ahi_im[2], ahi_im[3]);
+            st_shared_v4(A + chunk_off(128 + lane, group), a1_re[0], a1_re[1], a1_re[2], a1_re[3]);
+            st_shared_v4(A + chunk_off(160 + lane, group), a1_im[0], a1_im[1], a1_im[2], a1_im[3]);
+            st_shared_v4(B + chunk_off(lane, group), blo[0], blo[1], blo[2], blo[3]);
+            st_shared_v4(B + chunk_off(32 + lane, group), bhi[0], bhi[1], bhi[2], bhi[3]);
+            fence_proxy_async();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&full[s]);
+        }
+        // ---- epilogue: TMEM -> smem planes -> partial subgrid
+        const bool ok = warp_wait(accb, 0, abort_flag, kWaitNs);
+        tc_fence_after();
+        float *E = reinterpret_cast<float *>(smem);  // stage 0 is free once accb completed
+        const int q = warp & 3, half = warp >> 2;
+        const int plane = q < 2 ? q * 2 + half : (half == 1 ? 2 + q : -1);
+        if (ok && plane >= 0) {
+            uint32_t r[32];
+            tmem_ld32(tmem + (static_cast<uint32_t>(32 * q) << 16) + static_cast<uint32_t>(half * 32), r);
+            tmem_ld_wait();
+#pragma unroll
+            for (int j = 0; j < 32; j++) E[plane * 32 * 33 + lane * 33 + j] = __uint_as_float(r[j]);
+        }
+        tc_fence_before();
+        named_bar(1, kGProducerWarps * 32);
+        if (ok && !*abort_flag) {
+            float2 *out = a.partials + static_cast<int64_t>(it.slot) * kS * kS;
+            const float i0 = 1.f / sv, i1 = 1.f / (sv * sw);  // exact: powers of two
+            for (int p = threadIdx.x; p < kS * kS; p += kGProducerWarps * 32) {
+                const int y = p >> 5, x = p & 31;
+                const int e = y * 33 + x;
+                const float p0re = (E[0 * 1056 + e] + E[1 * 1056 + e]) * i0;
+                const float p0im = (E[2 * 1056 + e] + E[3 * 1056 + e]) * i0;
+                const float p1re = E[4 * 1056 + e] * i1, p1im = E[5 * 1056 + e] * i1;
+                const float rr = a.tabs[kS + p], tap = a.taper[p];
+                const float re = fmaf(-rr, p1im, p0re), im = fmaf(rr, p1re, p0im);
+                out[((y + kS / 2) % kS) * kS + (x + kS / 2) % kS] = make_float2(re * tap, im * tap);
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == kGProducerWarps) {
+        tc_fence_after();
+        tmem_dealloc(tmem, kGTmemCols);
+    }
+}
+
+// ---------------- degridder ----------------
+
+constexpr int kDTile = 128;
+constexpr int kDThreads = 9 * 32;  // warps 0-3 producers, 4-7 epilogue, 8 MMA
+constexpr uint32_t kDStatic = 192 * 64 * 2;
+constexpr uint32_t kDTileHalf = 128 * 64 * 2;  // hi (or lo) operand of one tile
+constexpr uint32_t kDTileBytes = 2 * kDTileHalf;
+constexpr uint32_t kDSmem = kDStatic + 2 * kDTileBytes + 256 + 256 + 1024;
+constexpr uint32_t kDTmemCols = 256;
+
+template <bool BF16, typename OutT>
+__global__ void __launch_bounds__(kDThreads, 2) tc_degridder_kernel(const TcArgs a) {
+    extern __shared__ unsigned char smem_raw[];
+    unsigned char *smem = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    unsigned char *bstat = smem;
+    unsigned char *tiles = smem + kDStatic;
+    float *tab_m = reinterpret_cast<float *>(tiles + 2 * kDTileBytes);  // m[32], g[32]
+    float *tab_g = tab_m + kS;
+    uint64_t *a_full = reinterpret_cast<uint64_t *>(tab_m + 2 * kS);
+    uint64_t *a_empty = a_full + 2;
+    uint64_t *acc_full = a_empty + 2;
+    uint64_t *acc_empty = acc_full + 2;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(acc_empty + 2);
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const Geometry &g = a.g;
+    const WorkItem it = a.items[blockIdx.x];
+    const DevSubgrid sg = a.subs[it.subgrid];
+    const int nvis = it.nt * g.nch;
+    const int ntiles = (nvis + kDTile - 1) / kDTile;
+    const int64_t cbase = a.coef_off[it.subgrid] + static_cast<int64_t>(it.t0 - sg.t0) * g.nch;
+
+    if (threadIdx.x == 0) {
+        for (int b = 0; b < 2; b++) {
+            mbar_init(&a_full[b], 4);
+            mbar_init(&a_empty[b], 1);
+            mbar_init(&acc_full[b], 1);
+            mbar_init(&acc_empty[b], 4);
+        }
+        *abort_flag = 0;
+        mbar_fence_init();
+    }
+    if (threadIdx.x < kS) {
+        tab_m[threadIdx.x] = a.lmn[threadIdx.x];
+        tab_g[threadIdx.x] = a.tabs[threadIdx.x];
+    }
+    if (warp == 8) {
+        tmem_alloc(tmem_slot, kDTmemCols);
+        tmem_relinquish();
+    }
+    // static B operand from the subgrid: rows (block, 2y+p), k = 2x + q
+    float sq = 1.f;  // FP16: power-of-two scale of this subgrid's pixels
+    if (warp < 8) {
+        const float2 *data = a.subgrids + static_cast<int64_t>(it.subgrid) * kS * kS;
+        if (!BF16) {
+            float mx = 0.f;
+            for (int pi = threadIdx.x; pi < kS * kS; pi += 256) {
+                const int y = pi >> 5, x = pi & 31;
+                const float2 d = data[((y + kS / 2) % kS) * kS + (x + kS / 2) % kS];
+                const float tap = fabsf(a.taper[pi]);
+                mx = fmaxf(mx, fmaxf(fabsf(d.x), fabsf(d.y)) * tap);
+            }
+            sq = pow2_scale(block256_max(mx, reinterpret_cast<float *>(tmem_slot + 2)));
+        }
+        const float sr = BF16 ? 1.f : a.r_scale;
+        const uint32_t bs = smem_u32(bstat);
+        for (int cc = threadIdx.x; cc < 192 * 8; cc += 256) {
+            const int cm = cc >> 3, r8 = cc & 7;
+            const int row = (cm >> 3) * 8 + r8, kg = cm & 7;
+            const int blk = row >> 6, rr = row & 63, y = rr >> 1, p = rr & 1;
+            uint32_t w[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int x = kg * 4 + u;
+                const int pi = y * kS + x;
+                const float2 d = data[((y + kS / 2) % kS) * kS + (x + kS / 2) % kS];
+                const float tap = a.taper[pi] * sq;
+                float qre = tap * d.x, qim = tap * d.y;
+                if (blk == 2) {
+                    const float rr2 = a.tabs[kS + pi] * sr;
+                    qre *= rr2;
+                    qim *= rr2;
+                }
+                // p = re: (Q_re, Q_im);  p = im: (Q_im, -Q_re)
+                const float e0 = p == 0 ? qre : qim, e1 = p == 0 ? qim : -qre;
+                uint32_t hi, lo;
+                split_pair<BF16>(e0, e1, hi, lo);
+                w[u] = blk == 0 ? lo : hi;
+            }
+            st_shared_v4(bs + cc * 16, w[0], w[1], w[2], w[3]);
+        }
+        fence_proxy_async();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+    const uint32_t bs = smem_u32(bstat), ts = smem_u32(tiles);
+
+    if (warp == 8) {
+        // ---- MMA issuer
+        if (lane == 0) {
+            constexpr uint32_t id128 = idesc_f16(128, 128, BF16), id64 = idesc_f16(128, 64, BF16);
+            for (int i = 0; i < ntiles; i++) {
+                const int b = i & 1;
+                const uint32_t ph = (i >> 1) & 1;
+                if (!mbar_wait(&a_full[b], ph, abort_flag, kWaitNs) ||
+                    !mbar_wait(&acc_empty[b], ph ^ 1, abort_flag, kWaitNs)) {
+                    *abort_flag = 1;
+                    atomicOr(a.status, kStatusWait);
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t ahi = ts + b * kDTileBytes, alo = ahi + kDTileHalf;
+                const uint32_t acc = tmem + static_cast<uint32_t>(b * 128);
+#pragma unroll
+                for (int kc = 0; kc < 4; kc++) {
+                    const uint64_t dahi = smem_desc(ahi + kc * 256, 128, 1024);
+                    mma_f16(acc, dahi, smem_desc(bs + 8 * 1024 + kc * 256, 128, 1024), id128, kc > 0 ? 1u : 0u);
+                    mma_f16(acc, dahi, smem_desc(bs + kc * 256, 128, 1024), id64, 1u);
+                    mma_f16(acc, smem_desc(alo + kc * 256, 128, 1024), smem_desc(bs + 8 * 1024 + kc * 256, 128, 1024),
+                            id64, 1u);
+                }
+                mma_commit(&a_empty[b]);
+                mma_commit(&acc_full[b]);
+            }
+            // drain: every issued MMA finished before the TMEM is released
+            mma_commit(&a_empty[0]);
+        }
+        __syncwarp();
+    } else if (warp < 4) {
+        // ---- producers: A tile (128 visibilities x 32 x), hi and lo
+        for (int i = 0; i < ntiles; i++) {
+            const int b = i & 1;
+            const uint32_t ph = (i >> 1) & 1;
+            if (!warp_wait(&a_empty[b], ph ^ 1, abort_flag, kWaitNs)) {
+                if (lane == 0) {
+                    *abort_flag = 1;
+                    atomicOr(a.status, kStatusWait);
+                }
+                break;
+            }
+            const uint32_t ahi = ts + b * kDTileBytes, alo = ahi + kDTileHalf;
+            for (int u = 0; u < 8; u++) {
+                const int cc = threadIdx.x + 128 * u;
+                const int cm = cc >> 3, r8 = cc & 7;
+                const int row = (cm >> 3) * 8 + r8, kg = cm & 7;
+                const int j = i * kDTile + row;
+                float4 c = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (j < nvis) c = a.coef[cbase + j];
+                uint32_t whi[4], wlo[4];
+#pragma unroll
+                for (int v = 0; v < 4; v++) {
+                    const int x = kg * 4 + v;
+                    float sa, ca;
+                    __sincosf(fmaf(c.x, tab_m[x], c.z * tab_g[x]), &sa, &ca);
+                    split_pair<BF16>(ca, sa, whi[v], wlo[v]);
+                }
+                st_shared_v4(ahi + cc * 16, whi[0], whi[1], whi[2], whi[3]);
+                st_shared_v4(alo + cc * 16, wlo[0], wlo[1], wlo[2], wlo[3]);
+            }
+            fence_proxy_async();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&a_full[b]);
+        }
+    } else {
+        // ---- epilogue: one visibility per thread
+        const int q = warp & 3;
+        OutT *out = static_cast<OutT *>(a.vis_out);
+        for (int i = 0; i < ntiles; i++) {
+            const int b = i & 1;
+            const uint32_t ph = (i >> 1) & 1;
+            if (!warp_wait(&acc_full[b], ph, abort_flag, kWaitNs)) {
+                if (lane == 0) {
+                    *abort_flag = 1;
+                    atomicOr(a.status, kStatusWait);
+                }
+                break;
+            }
+            tc_fence_after();
+            const int j = i * kDTile + q * 32 + lane;
+            float4 c = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (j < nvis) c = a.coef[cbase + j];
+            const float dwe = BF16 ? c.z : c.z / a.r_scale;  // T1 was formed from r * r_scale
+            const uint32_t acc = tmem + (static_cast<uint32_t>(32 * q) << 16) + static_cast<uint32_t>(b * 128);
+            float vre = 0.f, vim = 0.f;
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                uint32_t t0[32], t1[32];
+                tmem_ld32(acc + h * 32, t0);
+                tmem_ld32(acc + 64 + h * 32, t1);
+                tmem_ld_wait();
+#pragma unroll
+                for (int yy = 0; yy < 16; yy++) {
+                    const int y = h * 16 + yy;
+                    const float t0re = __uint_as_float(t0[2 * yy]), t0im = __uint_as_float(t0[2 * yy + 1]);
+                    const float t1re = __uint_as_float(t1[2 * yy]), t1im = __uint_as_float(t1[2 * yy + 1]);
+                    const float zre = fmaf(dwe, t1im, t0re), zim = fmaf(-dwe, t1re, t0im);
+                    float sb, cb;
+                    __sincosf(fmaf(c.y, tab_m[y], c.z * tab_g[y]), &sb, &cb);
+                    vre = fmaf(cb, zre, fmaf(sb, zim, vre));
+                    vim = fmaf(cb, zim, fmaf(-sb, zre, vim));
+                }
+            }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&acc_empty[b]);
+            if (j < nvis) {
+                const int t = it.t0 + j / g.nch, ch = j - (j / g.nch) * g.nch;
+                const float sc = g.inv_s2 / sq;  // exact: sq is a power of two
+                store_vis(out, (static_cast<int64_t>(sg.bl) * g.nt_all + t) * g.nch + ch,
+                          make_float2(vre * sc, vim * sc));
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 8) {
+        // wait (bounded) for the drain commit: all MMAs of this CTA are complete
+        if (lane == 0) {
+            const int nb0 = (ntiles + 1) / 2;  // completed phases of a_empty[0] before the drain
+            if (!mbar_wait(&a_empty[0], static_cast<uint32_t>(nb0 & 1), abort_flag, kWaitNs) && !*abort_flag)
+                atomicOr(a.status, kStatusWait);
+        }
+        __syncwarp();
+        tc_fence_after();
+        tmem_dealloc(tmem, kDTmemCols);
+    }
+}
+
+// ---------------- self-test GEMM: C[128][N] = A[128][64] . B[N][64]^T ----------------
+
+template <bool BF16>
+__global__ void __launch_bounds__(128) tc_selftest_kernel(const float *A, const float *B, int N, float *C,
+                                                          int32_t *status) {
+    extern __shared__ unsigned char smem_raw[];
+    unsigned char *smem = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    unsigned char *sa = smem, *sb = smem + 128 * 128;
+    uint64_t *bar = reinterpret_cast<uint64_t *>(sb + 128 * 128);
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bar + 1);
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (threadIdx.x == 0) {
+        mbar_init(bar, 1);
+        *abort_flag = 0;
+        mbar_fence_init();
+    }
+    if (warp == 0) {
+        tmem_alloc(tmem_slot, 128);
+        tmem_relinquish();
+    }
+    // operands: each 16-byte chunk (row, kg) holds 8 consecutive k of one row
+    for (int cc = threadIdx.x; cc < 128 * 8; cc += 128) {
+        const int row = (cc >> 6) * 8 + (cc & 7), kg = (cc >> 3) & 7;
+        uint32_t w[4];
+        for (int u = 0; u < 4; u++)
+            w[u] = Half16<BF16>::pack(A[row * 64 + kg * 8 + 2 * u], A[row * 64 + kg * 8 + 2 * u + 1]);
+        st_shared_v4(smem_u32(sa) + cc * 16, w[0], w[1], w[2], w[3]);
+        if (row < N) {
+            for (int u = 0; u < 4; u++)
+                w[u] = Half16<BF16>::pack(B[row * 64 + kg * 8 + 2 * u], B[row * 64 + kg * 8 + 2 * u + 1]);
+            st_shared_v4(smem_u32(sb) + cc * 16, w[0], w[1], w[2], w[3]);
+        }
+    }
+    fence_proxy_async();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+    if (threadIdx.x == 0) {
+        const uint32_t idesc = idesc_f16(128, N, BF16);
+        for (int kc = 0; kc < 4; kc++)
+            mma_f16(tmem, smem_desc(smem_u32(sa) + kc * 256, 128, 1024), smem_desc(smem_u32(sb) + kc * 256, 128, 1024),
+                    idesc, kc > 0 ? 1u : 0u);
+        mma_commit(bar);
+    }
+    __syncwarp();
+    const bool ok = warp_wait(bar, 0, abort_flag, kWaitNs);
+    if (!ok && lane == 0) atomicOr(status, kStatusWait);
+    tc_fence_after();
+    if (ok) {
+        for (int c0 = 0; c0 < N; c0 += 32) {
+            uint32_t r[32];
+            tmem_ld32(tmem + (static_cast<uint32_t>(32 * warp) << 16) + c0, r);
+            tmem_ld_wait();
+            for (int j = 0; j < 32; j++) C[(32 * warp + lane) * N + c0 + j] = __uint_as_float(r[j]);
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        tmem_dealloc(tmem, 128);
+    }
+}
+
+template <typename K>
+cudaError_t set_smem(K kernel, uint32_t bytes) {
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes));
+}
+
+void fill_args(TcArgs &t, const GridderArgs &a, const TcPlanState &st) {
+    t.g = a.g;
+    t.subs = a.subs;
+    t.coef_off = static_cast<const int64_t *>(st.coef_off);
+    t.coef = static_cast<const float4 *>(st.coef);
+    t.lmn = a.lmn;
+    t.tabs = static_cast<const float *>(st.tables);
+    t.taper = a.taper;
+    t.dw_scale = st.dw_scale;
+    t.r_scale = st.r_scale;
+}
+
+}  // namespace
+
+bool tc_subgrid_size_supported(int S) { return S == kS; }
+
+p9idg_status tc_prepare(TcPlanState &st, const std::vector<p9idg_subgrid> &subs, const std::vector<float> &lmn,
+                        int S, int nch, const std::vector<double> &wn, const double *uvw_host, int nt_all,
+                        cudaStream_t stream, std::string &err) {
+    if (st.ready) return P9IDG_OK;
+    if (S != kS) {
+        err = "tensor-core kernels support subgrid size 32 only";
+        return P9IDG_UNSUPPORTED;
+    }
+    // separable part of n and the remainder r (Gridder.cs:168-174 values in the lmn table)
+    std::vector<float> tabs(S + S * S);
+    for (int x = 0; x < S; x++) {
+        const double l = lmn[x], t = l * l;
+        tabs[x] = static_cast<float>(t / (t + std::sqrt(1.0 - t)));
+    }
+    double rmax = 0;
+    for (int y = 0; y < S; y++)
+        for (int x = 0; x < S; x++) {
+            const double r = static_cast<double>(lmn[S + y * S + x]) - tabs[x] - tabs[y];
+            tabs[S + y * S + x] = static_cast<float>(r);
+            rmax = std::max(rmax, std::fabs(r));
+        }
+    // coefficient offsets per subgrid and the largest |dw|
+    std::vector<int64_t> off(subs.size() + 1, 0);
+    double wmax = 0, kmax = 0;
+    for (double k : wn) kmax = std::max(kmax, std::fabs(k));
+    for (size_t i = 0; i < subs.size(); i++) {
+        off[i + 1] = off[i] + static_cast<int64_t>(subs[i].time_sample_count) * nch;
+        for (int t = 0; t < subs[i].time_sample_count; t++) {
+            const double w = uvw_host[(static_cast<int64_t>(subs[i].baseline_idx) * nt_all + subs[i].time_sample_start + t) * 3 + 2];
+            wmax = std::max(wmax, std::fabs(w));
+        }
+    }
+    st.max_w_r = wmax * kmax * rmax;
+    // powers of two keeping dw * B and r * pix inside the FP16 range (|woff| = 0, so |dw| <= k |w|)
+    auto pow2_below = [](double m) {
+        if (!(m > 0) || !std::isfinite(m)) return 1.f;
+        int e;
+        std::frexp(m, &e);
+        return static_cast<float>(std::ldexp(1.0, -e));
+    };
+    st.dw_scale = pow2_below(wmax * kmax * 1.0001);
+    st.r_scale = pow2_below(rmax);
+    if (st.max_w_r > 0.05) {
+        err = "w term too large for the first-order separable tensor-core form (|dw r| = " +
+              std::to_string(st.max_w_r) + ")";
+        return P9IDG_UNSUPPORTED;
+    }
+    // degridder work items: whole time samples, up to 2048 visibilities each
+    std::vector<DevSubgrid> dtmp;
+    std::vector<WorkItem> ditems;
+    build_work_items(subs, nch, 2048, dtmp, ditems);
+    st.ncoef = off.back();
+    cudaError_t e;
+    if ((e = cudaMalloc(&st.coef, sizeof(float4) * std::max<int64_t>(1, st.ncoef))) != cudaSuccess ||
+        (e = cudaMalloc(&st.coef_off, sizeof(int64_t) * off.size())) != cudaSuccess ||
+        (e = cudaMalloc(&st.tables, sizeof(float) * tabs.size())) != cudaSuccess ||
+        (e = cudaMalloc(&st.ditems, sizeof(WorkItem) * std::max<size_t>(1, ditems.size()))) != cudaSuccess) {
+        err = std::string("tensor-core buffers: ") + cudaGetErrorString(e);
+        tc_release(st);
+        return e == cudaErrorMemoryAllocation ? P9IDG_OUT_OF_MEMORY : P9IDG_CUDA_ERROR;
+    }
+    cudaMemcpyAsync(st.coef_off, off.data(), sizeof(int64_t) * off.size(), cudaMemcpyHostToDevice, stream);
+    cudaMemcpyAsync(st.tables, tabs.data(), sizeof(float) * tabs.size(), cudaMemcpyHostToDevice, stream);
+    if (!ditems.empty())
+        cudaMemcpyAsync(st.ditems, ditems.data(), sizeof(WorkItem) * ditems.size(), cudaMemcpyHostToDevice, stream);
+    if ((e = cudaStreamSynchronize(stream)) != cudaSuccess) {
+        err = std::string("tensor-core tables: ") + cudaGetErrorString(e);
+        return P9IDG_CUDA_ERROR;
+    }
+    st.nditems = static_cast<int32_t>(ditems.size());
+    st.S = S;
+    st.ready = true;
+    return P9IDG_OK;
+}
+
+static p9idg_status launch_coef(TcPlanState &st, const GridderArgs &a, int32_t nsub, cudaStream_t stream,
+                                std::string &err) {
+    if (nsub == 0) return P9IDG_OK;
+    tc_coef_kernel<<<nsub, 256, 0, stream>>>(a.subs, static_cast<const int64_t *>(st.coef_off), a.uvw, a.wavenumbers,
+                                             a.g, static_cast<float4 *>(st.coef));
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        err = std::string("coefficient kernel: ") + cudaGetErrorString(e);
+        return P9IDG_CUDA_ERROR;
+    }
+    return P9IDG_OK;
+}
+
+p9idg_status tc_grid(TcPlanState &st, const GridderArgs &a, int mode, cudaStream_t stream, std::string &err) {
+    if (!st.ready) {
+        err = "tensor-core state not prepared";
+        return P9IDG_INVALID_ARGUMENT;
+    }
+    p9idg_status s = launch_coef(st, a, a.nsub, stream, err);
+    if (s != P9IDG_OK || a.nitems == 0) return s;
+    TcArgs t{};
+    fill_args(t, a, st);
+    t.items = a.items;
+    t.vis = a.vis;
+    t.partials = a.partials;
+    t.status = a.status;
+    const bool bf16 = mode == P9IDG_MODE_TC_BF16X3;
+    cudaError_t e;
+    if (bf16 && a.vis_c128) {
+        e = set_smem(tc_gridder_kernel<true, double2>, kGSmem);
+        if (e == cudaSuccess) tc_gridder_kernel<true, double2><<<a.nitems, kGThreads, kGSmem, stream>>>(t);
+    } else if (bf16) {
+        e = set_smem(tc_gridder_kernel<true, float2>, kGSmem);
+        if (e == cudaSuccess) tc_gridder_kernel<true, float2><<<a.nitems, kGThreads, kGSmem, stream>>>(t);
+    } else if (a.vis_c128) {
+        e = set_smem(tc_gridder_kernel<false, double2>, kGSmem);
+        if (e == cudaSuccess) tc_gridder_kernel<false, double2><<<a.nitems, kGThreads, kGSmem, stream>>>(t);
+    } else {
+        e = set_smem(tc_gridder_kernel<false, float2>, kGSmem);
+        if (e == cudaSuccess) tc_gridder_kernel<false, float2><<<a.nitems, kGThreads, kGSmem, stream>>>(t);
+    }
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        err = std::string("tensor-core gridder: ") + cudaGetErrorString(e);
+        return P9IDG_CUDA_ERROR;
+    }
+    return P9IDG_OK;
+}
+
+p9idg_status tc_degrid(TcPlanState &st, const GridderArgs &a, int mode, cudaStream_t stream, std::string &err) {
+    if (!st.ready) {
+        err = "tensor-core state not prepared";
+        return P9IDG_INVALID_ARGUMENT;
+    }
+    p9idg_status s = launch_coef(st, a, a.nsub, stream, err);
+    if (s != P9IDG_OK || st.nditems == 0) return s;
+    TcArgs t{};
+    fill_args(t, a, st);
+    t.items = static_cast<const WorkItem *>(st.ditems);
+    t.subgrids = a.subgrids;
+    t.vis_out = a.vis_out;
+    t.status = a.status;
+    const bool bf16 = mode == P9IDG_MODE_TC_BF16X3;
+    cudaError_t e;
+    if (bf16 && a.out_c128) {
+        e = set_smem(tc_degridder_kernel<true, double2>, kDSmem);
+        if (e == cudaSuccess) tc_degridder_kernel<true, double2><<<st.nditems, kDThreads, kDSmem, stream>>>(t);
+    } else if (bf16) {
+        e = set_smem(tc_degridder_kernel<true, float2>, kDSmem);
+        if (e == cudaSuccess) tc_degridder_kernel<true, float2><<<st.nditems, kDThreads, kDSmem, stream>>>(t);
+    } else if (a.out_c128) {
+        e = set_smem(tc_degridder_kernel<false, double2>, kDSmem);
+        if (e == cudaSuccess) tc_degridder_kernel<false, double2><<<st.nditems, kDThreads, kDSmem, stream>>>(t);
+    } else {
+        e = set_smem(tc_degridder_kernel<false, float2>, kDSmem);
+        if (e == cudaSuccess) tc_degridder_kernel<false, float2><<<st.nditems, kDThreads, kDSmem, stream>>>(t);
+    }
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        err = std::string("tensor-core degridder: ") + cudaGetErrorString(e);
+        return P9IDG_CUDA_ERROR;
+    }
+    return P9IDG_OK;
 }
 
 void tc_release(TcPlanState &st) {
-    if (st.scratch) cudaFree(st.scratch);
-    st.scratch = nullptr;
-    st.scratch_bytes = 0;
+    if (st.coef) cudaFree(st.coef);
+    if (st.coef_off) cudaFree(st.coef_off);
+    if (st.tables) cudaFree(st.tables);
+    if (st.ditems) cudaFree(st.ditems);
+    st = TcPlanState();
+}
+
+p9idg_status tc_selftest(int mode, int N, double *max_rel_err, std::string &err) {
+    if (N != 32 && N != 64 && N != 128) {
+        err = "self-test N must be 32, 64 or 128";
+        return P9IDG_INVALID_ARGUMENT;
+    }
+    std::vector<float> A(128 * 64), B(128 * 64);
+    uint32_t seed = 12345;
+    auto rnd = [&]() {
+        seed = seed * 1664525u + 1013904223u;
+        return static_cast<float>((seed >> 8) & 0xFFFF) / 65536.0f - 0.5f;
+    };
+    for (auto &v : A) v = rnd();
+    for (auto &v : B) v = rnd();
+    // operands exactly representable in 16 bits so the product is exact up to FP32 accumulation
+    const bool bf16 = mode == P9IDG_MODE_TC_BF16X3;
+    for (auto *v : {&A, &B})
+        for (auto &x : *v) {
+            uint32_t u;
+            std::memcpy(&u, &x, 4);
+            u &= bf16 ? 0xFFFF0000u : 0xFFFFE000u;
+            std::memcpy(&x, &u, 4);
+        }
+    float *dA = nullptr, *dB = nullptr, *dC = nullptr;
+    int32_t *dS = nullptr;
+    cudaError_t e = cudaMalloc(&dA, A.size() * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&dB, B.size() * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&dC, 128 * N * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&dS, 4);
+    if (e == cudaSuccess) e = cudaMemcpy(dA, A.data(), A.size() * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(dB, B.data(), B.size() * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(dS, 0, 4);
+    const uint32_t smem = 2 * 128 * 128 + 64 + 1024;
+    if (e == cudaSuccess) {
+        if (bf16) {
+            e = set_smem(tc_selftest_kernel<true>, smem);
+            if (e == cudaSuccess) tc_selftest_kernel<true><<<1, 128, smem>>>(dA, dB, N, dC, dS);
+        } else {
+            e = set_smem(tc_selftest_kernel<false>, smem);
+            if (e == cudaSuccess) tc_selftest_kernel<false><<<1, 128, smem>>>(dA, dB, N, dC, dS);
+        }
+        if (e == cudaSuccess) e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    }
+    std::vector<float> C(128 * N);
+    int32_t status = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(C.data(), dC, C.size() * 4, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(&status, dS, 4, cudaMemcpyDeviceToHost);
+    cudaFree(dA);
+    cudaFree(dB);
+    cudaFree(dC);
+    cudaFree(dS);
+    if (e != cudaSuccess) {
+        err = std::string("self-test: ") + cudaGetErrorString(e);
+        return P9IDG_CUDA_ERROR;
+    }
+    if (status != 0) {
+        err = "self-test: a wait timed out";
+        return P9IDG_DEVICE_CHECK_FAILED;
+    }
+    double maxerr = 0, maxref = 0;
+    for (int i = 0; i < 128; i++)
+        for (int j = 0; j < N; j++) {
+            double ref = 0;
+            for (int k = 0; k < 64; k++) ref += static_cast<double>(A[i * 64 + k]) * B[j * 64 + k];
+            maxerr = std::max(maxerr, std::fabs(ref - C[i * N + j]));
+            maxref = std::max(maxref, std::fabs(ref));
+        }
+    *max_rel_err = maxerr / std::max(maxref, 1e-30);
+    return P9IDG_OK;
 }
 
 }  // namespace p9idg

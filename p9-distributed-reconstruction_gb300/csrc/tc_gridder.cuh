@@ -2,20 +2,37 @@
 #pragma once
 
 #include <string>
+#include <vector>
 
 #include "kernels.cuh"
 
 namespace p9idg {
 
-// Device buffers owned by a plan for the tensor-core kernels.
+// Per-plan state of the tensor-core kernels (device buffers and host-built tables).
 struct TcPlanState {
-    void *scratch = nullptr;
-    size_t scratch_bytes = 0;
+    bool ready = false;
+    int S = 0;
+    int64_t ncoef = 0;
+    void *coef = nullptr;         // float4 {du, dv, dw, 0} per gridded visibility, subgrid order
+    void *coef_off = nullptr;     // int64 per subgrid: first coefficient of the subgrid
+    void *tables = nullptr;       // float: f[S] (separable part of n), r[S*S] (remainder)
+    void *ditems = nullptr;       // degridder work items (<= 2048 visibilities)
+    int32_t nditems = 0;
+    double max_w_r = 0;           // max |dw| * max |r|: size of the neglected second-order term
+    float dw_scale = 1.f;         // FP16 mode: power of two with max |dw| * dw_scale < 1
+    float r_scale = 1.f;          // FP16 mode: power of two with max |r| * r_scale < 1
 };
 
 bool tc_subgrid_size_supported(int S);
+// Builds the tables and uploads them (once per plan).
+p9idg_status tc_prepare(TcPlanState &st, const std::vector<p9idg_subgrid> &subs, const std::vector<float> &lmn,
+                        int S, int nch, const std::vector<double> &wn, const double *uvw_host, int nt_all,
+                        cudaStream_t stream, std::string &err);
 p9idg_status tc_grid(TcPlanState &st, const GridderArgs &a, int mode, cudaStream_t stream, std::string &err);
 p9idg_status tc_degrid(TcPlanState &st, const GridderArgs &a, int mode, cudaStream_t stream, std::string &err);
 void tc_release(TcPlanState &st);
+// Known GEMM C[128][n] = A[128][64] B[n][64]^T through the tcgen05 operand layout and
+// descriptors; reports the largest error relative to max |C|.
+p9idg_status tc_selftest(int mode, int n, double *max_rel_err, std::string &err);
 
 }  // namespace p9idg

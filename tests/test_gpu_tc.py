@@ -1,0 +1,78 @@
+"""Tensor-core split-precision gridder/degridder (P9IDG_MODE_TC_BF16X3 / _FP16X3).
+
+Bar: relative L2 error <= 1e-4 against the FP64 oracle (the bound stated for the
+tensor-core form), for grids, degridded visibilities and the dirty image.  The GEMM
+self-test pins the tcgen05 operand layout, descriptors and TMEM read-out with exactly
+representable inputs (error at FP32 accumulation level).
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+from conftest import constants, oracle, pkg, rel_l2, workload
+
+pytestmark = pytest.mark.gpu
+TOL_TC = 1e-4
+MODES = [pytest.param(pkg.MODE_TC_BF16X3, id="bf16x3"), pytest.param(pkg.MODE_TC_FP16X3, id="fp16x3")]
+
+
+@pytest.mark.parametrize("mode", MODES)
+@pytest.mark.parametrize("n", [32, 64, 128])
+def test_tcgen05_gemm_selftest(need_gpu, mode, n):
+    err = ctypes.c_double(-1)
+    st = pkg._native.lib().p9idg_tc_selftest(mode, n, ctypes.byref(err))
+    assert st == 0, pkg._native.last_error()
+    assert 0 <= err.value < 1e-6
+
+
+def _setup(name, kw, mode):
+    obs, cd = workload(name, **kw)
+    c, cd = constants(cd)
+    part = pkg.Partitioner.CreatePartition(c, obs.uvw, obs.frequencies)
+    part.plan.set_mode(mode)
+    subs = oracle.partition(cd, obs.uvw, obs.frequencies)
+    return obs, c, cd, part, subs
+
+
+CASES = [("meerkat_3072", dict(n_ant=10, nt=300, nch=16)), ("small_256", dict(n_ant=8, nt=300, nch=8))]
+
+
+@pytest.mark.parametrize("mode", MODES)
+@pytest.mark.parametrize("name,kw", CASES)
+def test_tc_grid_w(need_gpu, mode, name, kw):
+    obs, c, cd, part, subs = _setup(name, kw, mode)
+    got = pkg.IDG.GridW(c, part, obs.vis, obs.uvw, obs.frequencies)
+    ref = oracle.idg_grid_w(cd, subs, obs.vis, obs.uvw, obs.frequencies)
+    assert rel_l2(got, ref) < TOL_TC
+    img = pkg.FFT.WStackIFFTFloat(got, cd["vis_count"])
+    assert rel_l2(img, oracle.wstack_ifft_float(ref, cd["vis_count"])) < TOL_TC
+
+
+@pytest.mark.parametrize("mode", MODES)
+@pytest.mark.parametrize("name,kw", CASES)
+def test_tc_degrid_w(need_gpu, mode, name, kw):
+    obs, c, cd, part, subs = _setup(name, kw, mode)
+    model = oracle.fft_forward_float(oracle.shift(obs.model_image.astype(np.float32)))
+    got = pkg.IDG.DeGridW(c, part, model.copy(), obs.uvw, obs.frequencies)
+    ref, _ = oracle.idg_degrid(cd, subs, model, obs.uvw, obs.frequencies, wstack=True)
+    assert rel_l2(got, ref) < TOL_TC
+
+
+def test_tc_non_w_and_psf(need_gpu):
+    obs, c, cd, part, subs = _setup("small_256", dict(n_ant=8, nt=300, nch=8), pkg.MODE_TC_BF16X3)
+    assert rel_l2(pkg.IDG.Grid(c, part, obs.vis, obs.uvw, obs.frequencies),
+                  oracle.idg_grid(cd, subs, obs.vis, obs.uvw, obs.frequencies)) < TOL_TC
+    flags = np.zeros(obs.vis.shape, bool)
+    g_ref = oracle.idg_grid(cd, subs, oracle.unit_vis(flags), obs.uvw, obs.frequencies)
+    psf_ref = oracle.shift(oracle.fft_backward_real(g_ref, cd["vis_count"]))
+    assert rel_l2(pkg.IDG.CalculatePSF(c, part, obs.uvw, flags, obs.frequencies), psf_ref) < TOL_TC
+
+
+def test_tc_rejects_other_subgrid_sizes():
+    obs, cd = workload("small_256", n_ant=4, nt=50, nch=4)
+    c, cd = constants(cd, subgrid_size=16, kernel_size=4)
+    part = pkg.Partitioner.CreatePartition(c, obs.uvw, obs.frequencies)
+    with pytest.raises(pkg.P9IDGError) as e:
+        part.plan.set_mode(pkg.MODE_TC_BF16X3)
+    assert e.value.code == 8
