@@ -183,13 +183,51 @@ def run_reference(args):
     return 0
 
 
+def time_mode(plan, pkg, mode, step, stream, steps, warmup, ws, clock_gpu=None):
+    """Warm-up, then K timed steps between CUDA events on the plan's stream (max over ranks)."""
+    import torch
+
+    plan.set_mode(MODES[mode])
+    for _ in range(max(3, warmup)):
+        step()
+    plan.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(clock_gpu) if clock_gpu is not None else None
+    if clocks:
+        clocks.start()
+    plan.reset_timing()
+    plan.enable_timing(True)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        step()
+    e1.record(stream)
+    e1.synchronize()
+    plan.synchronize()
+    clk = clocks.stop() if clocks else None
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    stages = plan.stage_times()
+    plan.enable_timing(False)
+    if ws > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms, stages, clk
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--mode", default="auto", choices=["auto"] + list(MODES))
+    ap.add_argument("--mode", default="auto", choices=["auto"] + list(MODES),
+                    help="headline kernels; auto = tensor-core BF16x3, with the FP32 kernels timed beside it")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--antennas", type=int, default=None,
@@ -214,21 +252,12 @@ def main():
     part = pkg.Partitioner.CreatePartition(c, obs.uvw, obs.frequencies)
     plan = part.plan
     info = plan.info()
-    mode_name = args.mode
-    if mode_name == "auto":
-        mode_name = "fp32"
-        for m in ("tc_bf16x3",):
-            try:
-                plan.set_mode(MODES[m])
-                mode_name = m
-                break
-            except pkg.P9IDGError:
-                pass
-    plan.set_mode(MODES[mode_name])
+    headline = "tc_bf16x3" if args.mode == "auto" else args.mode
+    compare = ["fp32"] if args.mode == "auto" else []
 
     stream = torch.cuda.Stream()
     plan.set_stream(stream.cuda_stream)
-    N, W = cd["grid_size"], cd["wlayer_count"]
+    N, W, S = cd["grid_size"], cd["wlayer_count"], cd["subgrid_size"]
     model_img = obs.model_image.astype(np.float32)
     model_grid = pkg.FFT.Forward(np.fft.ifftshift(model_img) if N % 2 == 0 else model_img)
     with torch.cuda.stream(stream):
@@ -236,51 +265,39 @@ def main():
         d_layers = torch.empty((W, N, N), dtype=torch.complex64, device="cuda")
         d_grid = torch.from_numpy(model_grid.astype(np.complex64)).cuda()
         d_out = torch.empty_like(d_vis)
+        d_img = torch.empty((N, N), dtype=torch.float32, device="cuda")
     stream.synchronize()
 
     def step():
         plan.grid_w_device(d_vis.data_ptr(), d_layers.data_ptr())
         plan.degrid_w_device(d_grid.data_ptr(), d_out.data_ptr())
 
-    for _ in range(max(3, args.warmup)):
-        step()
-    plan.synchronize()
-    if ws > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
-    clocks = ClockSampler(local)
-    clocks.start()
-    plan.reset_timing()
-    plan.enable_timing(True)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.steps):
-        step()
-    e1.record(stream)
-    e1.synchronize()
-    plan.synchronize()
-    clk = clocks.stop()
-    if ws > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1)
-    stages = plan.stage_times()
-    plan.enable_timing(False)
-    if ws > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
     gridded = info["gridded_visibilities"]
-    value = ws * 2 * gridded * args.steps / (ms * 1e-3) / 1e6
+    results = {}
+    for mode in compare + [headline]:  # headline last: its clocks are sampled
+        ms, stages, clk = time_mode(plan, pkg, mode, step, stream, args.steps, args.warmup, ws,
+                                    clock_gpu=local if mode == headline else None)
+        results[mode] = dict(ms=ms, stages=stages, clk=clk,
+                             value=ws * 2 * gridded * args.steps / (ms * 1e-3) / 1e6)
+    head = results[headline]
+    stages = head["stages"]
     launches = sum(n for (_, n) in stages.values()) - stages["h2d"][1] - stages["d2h"][1]
 
-    # roofline of the dominant kernel
-    S = cd["subgrid_size"]
+    # the full-grid w-layer FFT (FFT.WStackIFFTFloat + FFT.Shift), timed separately
+    plan.reset_timing()
+    plan.enable_timing(True)
+    for _ in range(3):
+        plan.wstack_image_device(d_layers.data_ptr(), d_img.data_ptr(), True)
+    layer_fft = plan.stage_times()["layer_fft"]
+    plan.enable_timing(False)
+    layer_fft_ms = layer_fft[0] / max(1, layer_fft[1])
+
+    # roofline of the dominant kernel of the headline path
     peaks, peak_src = measured_peaks()
     kern = max(("gridder", "degridder"), key=lambda k: stages[k][0])
     kt_ms = stages[kern][0] / max(1, stages[kern][1])
-    if mode_name == "fp32":
-        sincos_peak, fma_peak = pkg.measure_sincos_peak()
+    if headline == "fp32":
+        sincos_peak, _ = pkg.measure_sincos_peak()
         achieved = gridded * S * S / (kt_ms * 1e-3) / 1e9
         roofline = {"bound": "sfu", "achieved": achieved, "peak": sincos_peak / 1e9, "unit": "Gsincos/s",
                     "frac": achieved / (sincos_peak / 1e9), "traffic": traffic_per_launch(kern + "_fp32"),
@@ -288,13 +305,20 @@ def main():
                     "work_per_launch": f"{gridded} visibilities x {S * S} pixels, one sincos + 10 flop each"}
     else:
         achieved = gridded * 10 * S * S / (kt_ms * 1e-3) / 1e12
+        # tcgen05 work actually issued per visibility: gridder 2 MMAs (M128 N64 + M128 N32, K16) per
+        # 8 visibilities; degridder 3 MMAs (N128 + N64 + N64, K16) per 128 visibilities x 4 K chunks / 128
+        phys = (2 * 128 * 96 * 16 / 8) if kern == "gridder" else (2 * 128 * 256 * 64 / 128)
         roofline = {"bound": "tensor", "achieved": achieved, "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
-                    "frac": achieved / peaks["bf16_tflops"], "traffic": traffic_per_launch(kern + "_" + mode_name),
-                    "kernel": kern + "_" + mode_name, "peak_source": f"{peak_src} bf16 dense (MEASURED_PEAKS.json)",
-                    "work_per_launch": f"{gridded} visibilities x {S * S} pixels x 10 algorithmic flop"}
-    stage_ms = {k: round(v[0] / max(1, v[1]), 4) for k, v in stages.items() if v[1]}
+                    "frac": achieved / peaks["bf16_tflops"], "traffic": traffic_per_launch(kern + "_" + headline),
+                    "kernel": kern + "_" + headline,
+                    "peak_source": f"{peak_src} dense bf16 (MEASURED_PEAKS.json bf16_tflops)",
+                    "work_per_launch": f"{gridded} visibilities x {S * S} pixels x 10 algorithmic flop",
+                    "physical_mma_tflops": gridded * phys / (kt_ms * 1e-3) / 1e12,
+                    "physical_mma_frac": gridded * phys / (kt_ms * 1e-3) / 1e12 / peaks["bf16_tflops"],
+                    "note": "algorithmic flop counts one complex MAC + phase per pixel and visibility (the FP32 "
+                            "kernel's work); the tensor-core kernels issue the physical MMA flop instead"}
 
-    # e2e through the reference-facing host API with pinned host buffers
+    # e2e through the reference-facing host API (IDG.GridW + IDG.DeGridW) with pinned host buffers
     e2e = None
     if not args.no_e2e:
         pin = lambda shape, dt: torch.empty(shape, dtype=dt, pin_memory=True).numpy()  # noqa: E731
@@ -302,19 +326,18 @@ def main():
         h_vis[...] = obs.vis
         h_uvw = pin(obs.uvw.shape, torch.float64)
         h_uvw[...] = obs.uvw
-        h_layers = pin((W, N, N), torch.complex128)
         h_grid = pin((N, N), torch.complex128)
         h_grid[...] = model_grid
+        plan.set_mode(MODES[headline])
         plan.set_stream(0)
         pkg.IDG.GridW(c, part, h_vis, h_uvw, obs.frequencies)  # warm-up of the host path buffers
         pkg.IDG.DeGridW(c, part, h_grid, h_uvw, obs.frequencies)
         steps_e2e = max(1, min(args.steps, 3))
         t0 = time.perf_counter()
         for _ in range(steps_e2e):
-            lay = pkg.IDG.GridW(c, part, h_vis, h_uvw, obs.frequencies)
-            v = pkg.IDG.DeGridW(c, part, h_grid, h_uvw, obs.frequencies)
+            pkg.IDG.GridW(c, part, h_vis, h_uvw, obs.frequencies)
+            pkg.IDG.DeGridW(c, part, h_grid, h_uvw, obs.frequencies)
         t_e2e = time.perf_counter() - t0
-        del lay, v
         nvis = obs.vis.size
         h2d = nvis * 16 + 2 * obs.uvw.nbytes + N * N * 16
         d2h = W * N * N * 16 + N * N * 16 + nvis * 16
@@ -327,37 +350,45 @@ def main():
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         oracle = load_oracle()
         subs = plan.subgrids()
-        mg = model_grid
-        sample, nv, _ = calibrate_cpu_sample(oracle, cd, subs, obs, mg, 12.0)
+        sample, nv, _ = calibrate_cpu_sample(oracle, cd, subs, obs, model_grid, 12.0)
         t0 = time.perf_counter()
-        layers_ref, vis_ref = cpu_reference_step(oracle, cd, sample, obs, mg)
+        layers_ref, vis_ref = cpu_reference_step(oracle, cd, sample, obs, model_grid)
         t_cpu = time.perf_counter() - t0
-        # accuracy of the GPU path on the same sample (plan restricted to the sampled subgrids)
-        sp = pkg.plan_from_subgrids(c, sample, obs.uvw, obs.frequencies)
-        sp.set_mode(MODES[mode_name])
-        spart = pkg.Partition([[]], sp)
-        lay_gpu = pkg.IDG.GridW(c, spart, obs.vis, obs.uvw, obs.frequencies)
-        vis_gpu = pkg.IDG.DeGridW(c, spart, mg.copy(), obs.uvw, obs.frequencies)
+        # accuracy of each GPU mode on the same sample (plan restricted to the sampled subgrids)
         rl = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))  # noqa: E731
+        acc = {}
+        for mode in [headline] + compare:
+            sp = pkg.plan_from_subgrids(c, sample, obs.uvw, obs.frequencies)
+            sp.set_mode(MODES[mode])
+            spart = pkg.Partition([[]], sp)
+            lay_gpu = pkg.IDG.GridW(c, spart, obs.vis, obs.uvw, obs.frequencies)
+            vis_gpu = pkg.IDG.DeGridW(c, spart, model_grid.copy(), obs.uvw, obs.frequencies)
+            acc[mode] = {"grid_w": rl(lay_gpu, layers_ref), "degrid_w": rl(vis_gpu, vis_ref)}
+            sp.destroy()
         cpu = {"value": 2 * nv / t_cpu / 1e6, "unit": "Mvis/s", "cores": oracle.num_threads(), "kind": "port",
                "sample": f"{len(sample)} of {len(subs)} subgrids ({nv} of {gridded} gridded visibilities), "
                          f"GridW + DeGridW of the sample in FP64",
-               "rel_l2_vs_fp64": {"grid_w": rl(lay_gpu, layers_ref), "degrid_w": rl(vis_gpu, vis_ref),
-                                  "mode": mode_name, "visibilities": nv}}
+               "rel_l2_vs_fp64": dict(acc, visibilities=nv)}
 
     if rank == 0:
-        out = {"metric": METRIC, "value": value, "unit": "Mvis/s", "n_gpus": ws, "steps": args.steps,
-               "warmup": max(3, args.warmup), "ms_per_step": ms / args.steps, "higher_is_better": True,
-               "scaling": "weak", "vs_baseline": None, "dtype": "f32" if mode_name == "fp32" else mode_name,
+        modes = {m: {"value": r["value"], "ms_per_step": r["ms"] / args.steps,
+                     "per_stage_ms": {k: round(v[0] / max(1, v[1]), 4) for k, v in r["stages"].items() if v[1]}}
+                 for m, r in results.items()}
+        out = {"metric": METRIC, "value": head["value"], "unit": "Mvis/s", "n_gpus": ws, "steps": args.steps,
+               "warmup": max(3, args.warmup), "ms_per_step": head["ms"] / args.steps, "higher_is_better": True,
+               "scaling": "weak", "vs_baseline": None, "dtype": "f32" if headline == "fp32" else headline,
                "data": "synthetic (seeded; stands in for the reference's MeerKAT FITS data, absent)",
                "config": {"workload": "3072^2 IDG grid+degrid: 2016 bl x 2000 t x 16 ch (64.5M vis), S=32, W=8",
-                          "mode": mode_name, "input_visibilities": info["input_visibilities"],
+                          "mode": headline, "input_visibilities": info["input_visibilities"],
                           "gridded_visibilities": gridded, "subgrids": info["num_subgrids"],
-                          "l2_flush": "inputs larger than L2 (vis 1.03 GB, layers 604 MB complex64)",
+                          "l2_flush": "inputs larger than L2 (vis 516 MB, layers 604 MB complex64)",
                           "value_counts": "gridded visibilities x 2 (gridder + degridder) per step",
-                          "per_stage_ms": stage_ms},
+                          "layer_fft_ms": round(layer_fft_ms, 4)},
+               "modes": modes,
+               "tc_over_fp32": (head["value"] / results["fp32"]["value"]) if "fp32" in results and
+               headline != "fp32" else None,
                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
-               "clocks": clk}
+               "clocks": head["clk"]}
         print(json.dumps(out), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()

@@ -118,6 +118,7 @@ struct p9idg_plan {
     std::vector<DevSubgrid> dsub;
     std::vector<WorkItem> gitems, ditems;
     int32_t nslots = 0;
+    bool items_dirty = true;  // gridder items / subgrid list not yet on the device
     int64_t gridded_vis = 0;
     std::vector<float> lmn, taper;
     std::vector<float> add_phasor;  // interleaved float2 [S][S]
@@ -211,16 +212,23 @@ p9idg_status check_params(const p9idg_params *c) {
     return P9IDG_OK;
 }
 
+// Gridder work items keep whole time samples: up to 1024 visibilities for the FP32 kernel,
+// 4096 for the tensor-core kernel (its per-item epilogue is heavier).  The subgrid list
+// records each subgrid's item slots for the subgrid IFFT + adder.
+void build_gridder_items(p9idg_plan *p) {
+    build_work_items(p->subs, p->nch, p->mode == P9IDG_MODE_FP32 ? 1024 : 4096, p->dsub, p->gitems);
+    p->nslots = 0;
+    for (const auto &d : p->dsub) p->nslots += d.item_count;
+    p->items_dirty = true;
+}
+
 void finish_plan(p9idg_plan *p) {
     const int S = p->c.subgrid_size;
-    // Gridder keeps whole time samples per item: up to ~1024 visibilities per item,
-    // degridder up to 512 (4 per thread of a 128-thread block).
+    // degridder items: up to 512 visibilities (4 per thread of a 128-thread block)
     std::vector<DevSubgrid> tmp;
-    build_work_items(p->subs, p->nch, 1024, p->dsub, p->gitems);
+    build_gridder_items(p);
     build_work_items(p->subs, p->nch, 512, tmp, p->ditems);
-    p->nslots = 0;
     p->gridded_vis = 0;
-    for (const auto &d : p->dsub) p->nslots += d.item_count;
     for (const auto &s : p->subs) p->gridded_vis += static_cast<int64_t>(s.time_sample_count) * p->nch;
     const float img = image_size(p->c);
     p->lmn.assign(S + S * S, 0.f);
@@ -254,8 +262,6 @@ p9idg_status ensure_device(p9idg_plan *p) {
     if (!p->stream) p->stream = p->own_stream;
     const int S = p->c.subgrid_size;
     CK(p->d_wn.ensure(sizeof(double) * std::max(1, p->nch)));
-    CK(p->d_sub.ensure(sizeof(DevSubgrid) * std::max<size_t>(1, p->dsub.size())));
-    CK(p->d_gitems.ensure(sizeof(WorkItem) * std::max<size_t>(1, p->gitems.size())));
     CK(p->d_ditems.ensure(sizeof(WorkItem) * std::max<size_t>(1, p->ditems.size())));
     CK(p->d_lmn.ensure(sizeof(float) * p->lmn.size()));
     CK(p->d_taper.ensure(sizeof(float) * S * S));
@@ -263,11 +269,6 @@ p9idg_status ensure_device(p9idg_plan *p) {
     CK(p->d_status.ensure(sizeof(int32_t)));
     cudaStream_t st = p->stream;
     CK(cudaMemcpyAsync(p->d_wn.p, p->wn.data(), sizeof(double) * p->nch, cudaMemcpyHostToDevice, st));
-    if (!p->dsub.empty())
-        CK(cudaMemcpyAsync(p->d_sub.p, p->dsub.data(), sizeof(DevSubgrid) * p->dsub.size(), cudaMemcpyHostToDevice, st));
-    if (!p->gitems.empty())
-        CK(cudaMemcpyAsync(p->d_gitems.p, p->gitems.data(), sizeof(WorkItem) * p->gitems.size(),
-                           cudaMemcpyHostToDevice, st));
     if (!p->ditems.empty())
         CK(cudaMemcpyAsync(p->d_ditems.p, p->ditems.data(), sizeof(WorkItem) * p->ditems.size(),
                            cudaMemcpyHostToDevice, st));
@@ -288,16 +289,33 @@ p9idg_status upload_uvw(p9idg_plan *p, const double *uvw) {
         StageScope t(p, P9IDG_STAGE_H2D);
         CK(cudaMemcpyAsync(p->d_uvw.p, uvw, bytes, cudaMemcpyHostToDevice, p->stream));
         p->uvw_uploaded = (uvw == p->uvw.data());
+        p->tc.coef_valid = false;
     } else if (!p->uvw_uploaded) {
         StageScope t(p, P9IDG_STAGE_H2D);
         CK(cudaMemcpyAsync(p->d_uvw.p, p->uvw.data(), bytes, cudaMemcpyHostToDevice, p->stream));
         p->uvw_uploaded = true;
+        p->tc.coef_valid = false;
     }
+    return P9IDG_OK;
+}
+
+p9idg_status upload_items(p9idg_plan *p) {
+    CK(p->d_sub.ensure(sizeof(DevSubgrid) * std::max<size_t>(1, p->dsub.size())));
+    CK(p->d_gitems.ensure(sizeof(WorkItem) * std::max<size_t>(1, p->gitems.size())));
+    if (!p->dsub.empty())
+        CK(cudaMemcpyAsync(p->d_sub.p, p->dsub.data(), sizeof(DevSubgrid) * p->dsub.size(), cudaMemcpyHostToDevice,
+                           p->stream));
+    if (!p->gitems.empty())
+        CK(cudaMemcpyAsync(p->d_gitems.p, p->gitems.data(), sizeof(WorkItem) * p->gitems.size(),
+                           cudaMemcpyHostToDevice, p->stream));
+    CK(cudaStreamSynchronize(p->stream));  // the host vectors may be rebuilt by a later set_mode
+    p->items_dirty = false;
     return P9IDG_OK;
 }
 
 p9idg_status prepare(p9idg_plan *p, const double *uvw) {
     TRY(ensure_device(p));
+    if (p->items_dirty) TRY(upload_items(p));
     if (p->taper_dirty) {
         CK(cudaMemcpyAsync(p->d_taper.p, p->taper.data(), sizeof(float) * p->taper.size(), cudaMemcpyHostToDevice,
                            p->stream));
@@ -646,7 +664,9 @@ p9idg_status p9idg_plan_set_mode(p9idg_plan *plan, int32_t mode) {
         return fail(P9IDG_UNSUPPORTED, "subgrid size not supported by the FP32 kernels");
     if (mode != P9IDG_MODE_FP32 && !tc_subgrid_size_supported(plan->c.subgrid_size))
         return fail(P9IDG_UNSUPPORTED, "subgrid size not supported by the tensor-core kernels");
+    const bool regroup = (plan->mode == P9IDG_MODE_FP32) != (mode == P9IDG_MODE_FP32);
     plan->mode = mode;
+    if (regroup) build_gridder_items(plan);
     return P9IDG_OK;
 }
 

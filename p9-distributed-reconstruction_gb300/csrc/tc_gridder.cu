@@ -85,6 +85,8 @@ __device__ __forceinline__ void split_pair(float a, float b, uint32_t &hi, uint3
 __device__ __forceinline__ uint32_t neg_hi(uint32_t w) { return w ^ 0x80000000u; }
 __device__ __forceinline__ uint32_t swap_halves(uint32_t w) { return (w >> 16) | (w << 16); }
 
+// The "memory" clobber keeps global loads from moving across these stores, so the kernels
+// prefetch the next stage's inputs into registers explicitly before storing this one.
 __device__ __forceinline__ void st_shared_v4(uint32_t addr, uint32_t a, uint32_t b, uint32_t c, uint32_t d) {
     asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(a), "r"(b), "r"(c), "r"(d)
                  : "memory");
@@ -159,26 +161,39 @@ __global__ void tc_coef_kernel(const DevSubgrid *subs, const int64_t *coef_off, 
 }
 
 // ---------------- gridder ----------------
+//
+// Warps 0-7 produce the MMA operands (warp = 4 visibilities of a stage = one k group; lane =
+// y for the A side and x for the B side), warp 8 issues the MMAs, warp 9 streams each stage's
+// 32 coefficients and visibilities into a shared-memory ring with cp.async so the producers
+// never wait on global memory.
 
 constexpr int kGVps = 32;      // visibilities per pipeline stage (K = 64)
 constexpr int kGStages = 3;
 constexpr int kGProducerWarps = 8;
-constexpr int kGThreads = (kGProducerWarps + 1) * 32;
+constexpr int kGMmaWarp = 8;
+constexpr int kGLoaderWarp = 9;
+constexpr int kGThreads = 10 * 32;
+constexpr int kGRing = 8;                          // input ring depth (stages)
+constexpr uint32_t kGRingSlot = 32 * 16 + 32 * 16;  // coefficients + visibilities (complex128 at most)
 constexpr uint32_t kGStageA = 192 * 64 * 2;
 constexpr uint32_t kGStageB = 64 * 64 * 2;
 constexpr uint32_t kGStageBytes = kGStageA + kGStageB;
-constexpr uint32_t kGSmem = kGStages * kGStageBytes + 256 + 1024;  // + barriers + alignment slack
+constexpr uint32_t kGSmem = kGStages * kGStageBytes + kGRing * kGRingSlot + 512 + 1024;
 constexpr uint32_t kGTmemCols = 64;
 
 template <bool BF16, typename VisT>
 __global__ void __launch_bounds__(kGThreads, 2) tc_gridder_kernel(const TcArgs a) {
     extern __shared__ unsigned char smem_raw[];
     unsigned char *smem = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-    uint64_t *full = reinterpret_cast<uint64_t *>(smem + kGStages * kGStageBytes);
+    unsigned char *ring = smem + kGStages * kGStageBytes;
+    uint64_t *full = reinterpret_cast<uint64_t *>(ring + kGRing * kGRingSlot);
     uint64_t *empty = full + kGStages;
     uint64_t *accb = empty + kGStages;
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(accb + 1);
+    uint64_t *in_full = accb + 1;
+    uint64_t *in_empty = in_full + kGRing;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(in_empty + kGRing);
     volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
+    float *red = reinterpret_cast<float *>(tmem_slot + 2);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const Geometry &g = a.g;
@@ -186,17 +201,24 @@ __global__ void __launch_bounds__(kGThreads, 2) tc_gridder_kernel(const TcArgs a
     const DevSubgrid sg = a.subs[it.subgrid];
     const int nvis = it.nt * g.nch;
     const int nstages = (nvis + kGVps - 1) / kGVps;
+    // an item is a run of whole time samples: its visibilities and coefficients are contiguous
+    const VisT *vrow = static_cast<const VisT *>(a.vis) + (static_cast<int64_t>(sg.bl) * g.nt_all + it.t0) * g.nch;
+    const float4 *crow = a.coef + a.coef_off[it.subgrid] + static_cast<int64_t>(it.t0 - sg.t0) * g.nch;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < kGStages; s++) {
             mbar_init(&full[s], kGProducerWarps);
             mbar_init(&empty[s], 1);
         }
+        for (int s = 0; s < kGRing; s++) {
+            mbar_init(&in_full[s], 32);                  // one cp.async arrival per loader lane
+            mbar_init(&in_empty[s], kGProducerWarps);
+        }
         mbar_init(accb, 1);
         *abort_flag = 0;
         mbar_fence_init();
     }
-    if (warp == kGProducerWarps) {
+    if (warp == kGMmaWarp) {
         tmem_alloc(tmem_slot, kGTmemCols);
         tmem_relinquish();
     }
@@ -204,9 +226,9 @@ __global__ void __launch_bounds__(kGThreads, 2) tc_gridder_kernel(const TcArgs a
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
-    const uint32_t sbase = smem_u32(smem);
+    const uint32_t sbase = smem_u32(smem), rbase = smem_u32(ring);
 
-    if (warp == kGProducerWarps) {
+    if (warp == kGMmaWarp) {
         // ---- MMA issuer ----
         if (lane == 0) {
             constexpr uint32_t id32 = idesc_f16(128, 32, BF16), id64 = idesc_f16(128, 64, BF16);
@@ -234,28 +256,74 @@ __global__ void __launch_bounds__(kGThreads, 2) tc_gridder_kernel(const TcArgs a
             if (!mbar_wait(accb, 0, abort_flag, kWaitNs)) atomicOr(a.status, kStatusWait);
         }
         __syncwarp();
+    } else if (warp == kGLoaderWarp) {
+        // ---- loader: stage i's 32 coefficients and visibilities -> ring slot i % kGRing
+        for (int i = 0; i < nstages; i++) {
+            const int slot = i % kGRing;
+            const uint32_t ph = (i / kGRing) & 1;
+            if (!warp_wait(&in_empty[slot], ph ^ 1, abort_flag, kWaitNs)) {
+                if (lane == 0) {
+                    *abort_flag = 1;
+                    atomicOr(a.status, kStatusWait);
+                }
+                break;
+            }
+            const int j = i * kGVps + lane;
+            const bool in = j < nvis;
+            const uint32_t dst = rbase + slot * kGRingSlot;
+            cp_async_16(dst + lane * 16, in ? crow + j : crow, in ? 16u : 0u);
+            if (sizeof(VisT) == 16)
+                cp_async_16(dst + 512 + lane * 16, in ? vrow + j : vrow, in ? 16u : 0u);
+            else
+                cp_async_8(dst + 512 + lane * 8, in ? vrow + j : vrow, in ? 8u : 0u);
+            cp_async_arrive(&in_full[slot]);
+        }
+        asm volatile("cp.async.wait_all;" ::: "memory");
     } else {
-        // ---- producers: 8 warps; warp = group of 4 visibilities (k group), lane = y (A side) and x (B side)
+        // ---- producers
         const int group = warp;
         const float m_y = a.lmn[lane], g_y = a.tabs[lane];  // y-side tables (l and m coincide, f and g coincide)
         const float l_x = m_y, f_x = g_y;
-        const VisT *vis = static_cast<const VisT *>(a.vis);
-        const int64_t cbase = a.coef_off[it.subgrid] + static_cast<int64_t>(it.t0 - sg.t0) * g.nch;
-        float *red = reinterpret_cast<float *>(tmem_slot + 2);
+        float ep_r[4], ep_t[4];  // remainder r and taper of the 4 pixels this thread finishes
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const int p = threadIdx.x + k * kGProducerWarps * 32;
+            ep_r[k] = a.tabs[kS + p];
+            ep_t[k] = a.taper[p];
+        }
         float sv = 1.f;  // FP16: power-of-two scale of this item's visibilities
         if (!BF16) {
             float mx = 0.f;
             for (int j = threadIdx.x; j < nvis; j += kGProducerWarps * 32) {
-                const int t = it.t0 + j / g.nch, ch = j - (j / g.nch) * g.nch;
-                const float2 v = load_vis(vis, (static_cast<int64_t>(sg.bl) * g.nt_all + t) * g.nch + ch);
+                const float2 v = load_vis(vrow, j);
                 mx = fmaxf(mx, fmaxf(fabsf(v.x), fabsf(v.y)));
             }
             sv = pow2_scale(block256_max(mx, red));
         }
         const float sw = BF16 ? 1.f : a.dw_scale;
         for (int i = 0; i < nstages; i++) {
-            const int s = i % kGStages;
-            const uint32_t ph = (i / kGStages) & 1;
+            const int s = i % kGStages, slot = i % kGRing;
+            const uint32_t ph = (i / kGStages) & 1, iph = (i / kGRing) & 1;
+            if (!warp_wait(&in_full[slot], iph, abort_flag, kWaitNs)) {
+                if (lane == 0) {
+                    *abort_flag = 1;
+                    atomicOr(a.status, kStatusWait);
+                }
+                break;
+            }
+            float4 c[4];
+            float2 vv[4];
+            {
+                const float4 *rc = reinterpret_cast<const float4 *>(ring + slot * kGRingSlot) + group * 4;
+                const VisT *rv = reinterpret_cast<const VisT *>(ring + slot * kGRingSlot + 512) + group * 4;
+#pragma unroll
+                for (int v = 0; v < 4; v++) {
+                    c[v] = rc[v];
+                    vv[v] = load_vis(rv, v);
+                }
+            }
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&in_empty[slot]);
             if (!warp_wait(&empty[s], ph ^ 1, abort_flag, kWaitNs)) {
                 if (lane == 0) {
                     *abort_flag = 1;
@@ -266,31 +334,23 @@ __global__ void __launch_bounds__(kGThreads, 2) tc_gridder_kernel(const TcArgs a
             uint32_t alo_re[4], alo_im[4], ahi_re[4], ahi_im[4], a1_re[4], a1_im[4], bhi[4], blo[4];
 #pragma unroll
             for (int v = 0; v < 4; v++) {
-                const int j = i * kGVps + group * 4 + v;
-                float4 c = make_float4(0.f, 0.f, 0.f, 0.f);
-                float2 vv = make_float2(0.f, 0.f);
-                if (j < nvis) {
-                    c = a.coef[cbase + j];
-                    const int t = it.t0 + j / g.nch, ch = j - (j / g.nch) * g.nch;
-                    vv = load_vis(vis, (static_cast<int64_t>(sg.bl) * g.nt_all + t) * g.nch + ch);
-                }
                 // y side: B_k(y)
                 float sb, cb;
-                __sincosf(fmaf(c.y, m_y, c.z * g_y), &sb, &cb);
+                __sincosf(fmaf(c[v].y, m_y, c[v].z * g_y), &sb, &cb);
                 uint32_t hi, lo;
                 split_pair<BF16>(cb, sb, hi, lo);  // hi = (hre, him), lo = (lre, lim)
                 ahi_re[v] = neg_hi(hi);                 // (hre, -him)
                 ahi_im[v] = swap_halves(hi);            // (him, hre)
                 alo_re[v] = neg_hi(lo);
                 alo_im[v] = swap_halves(lo);
-                const float dws = c.z * sw;
+                const float dws = c[v].z * sw;
                 const uint32_t h1 = Half16<BF16>::pack(dws * cb, dws * sb);
                 a1_re[v] = neg_hi(h1);
                 a1_im[v] = swap_halves(h1);
                 // x side: W = vis * A_k(x)
                 float sa, ca;
-                __sincosf(fmaf(c.x, l_x, c.z * f_x), &sa, &ca);
-                const float wre = (vv.x * ca - vv.y * sa) * sv, wim = (vv.x * sa + vv.y * ca) * sv;
+                __sincosf(fmaf(c[v].x, l_x, c[v].z * f_x), &sa, &ca);
+                const float wre = (vv[v].x * ca - vv[v].y * sa) * sv, wim = (vv[v].x * sa + vv[v].y * ca) * sv;
                 split_pair<BF16>(wre, wim, bhi[v], blo[v]);
             }
             const uint32_t A = sbase + s * kGStageBytes, B = A + kGStageA;
@@ -324,13 +384,15 @@ __global__ void __launch_bounds__(kGThreads, 2) tc_gridder_kernel(const TcArgs a
         if (ok && !*abort_flag) {
             float2 *out = a.partials + static_cast<int64_t>(it.slot) * kS * kS;
             const float i0 = 1.f / sv, i1 = 1.f / (sv * sw);  // exact: powers of two
-            for (int p = threadIdx.x; p < kS * kS; p += kGProducerWarps * 32) {
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const int p = threadIdx.x + k * kGProducerWarps * 32;
                 const int y = p >> 5, x = p & 31;
                 const int e = y * 33 + x;
                 const float p0re = (E[0 * 1056 + e] + E[1 * 1056 + e]) * i0;
                 const float p0im = (E[2 * 1056 + e] + E[3 * 1056 + e]) * i0;
                 const float p1re = E[4 * 1056 + e] * i1, p1im = E[5 * 1056 + e] * i1;
-                const float rr = a.tabs[kS + p], tap = a.taper[p];
+                const float rr = ep_r[k], tap = ep_t[k];
                 const float re = fmaf(-rr, p1im, p0re), im = fmaf(rr, p1re, p0im);
                 out[((y + kS / 2) % kS) * kS + (x + kS / 2) % kS] = make_float2(re * tap, im * tap);
             }
@@ -338,20 +400,28 @@ __global__ void __launch_bounds__(kGThreads, 2) tc_gridder_kernel(const TcArgs a
     }
     tc_fence_before();
     __syncthreads();
-    if (warp == kGProducerWarps) {
+    if (warp == kGMmaWarp) {
         tc_fence_after();
         tmem_dealloc(tmem, kGTmemCols);
     }
 }
 
 // ---------------- degridder ----------------
+//
+// Warps 0-3 produce the A tile (128 visibilities x 32 x phasors), warps 4-7 turn the
+// accumulators into visibilities, warp 8 issues the MMAs, warp 9 streams each tile's 128
+// coefficients into a shared-memory ring with cp.async.
 
 constexpr int kDTile = 128;
-constexpr int kDThreads = 9 * 32;  // warps 0-3 producers, 4-7 epilogue, 8 MMA
+constexpr int kDMmaWarp = 8;
+constexpr int kDLoaderWarp = 9;
+constexpr int kDThreads = 10 * 32;
+constexpr int kDRing = 4;
+constexpr uint32_t kDRingSlot = kDTile * 16;
 constexpr uint32_t kDStatic = 192 * 64 * 2;
 constexpr uint32_t kDTileHalf = 128 * 64 * 2;  // hi (or lo) operand of one tile
 constexpr uint32_t kDTileBytes = 2 * kDTileHalf;
-constexpr uint32_t kDSmem = kDStatic + 2 * kDTileBytes + 256 + 256 + 1024;
+constexpr uint32_t kDSmem = kDStatic + 2 * kDTileBytes + kDRing * kDRingSlot + 256 + 512 + 1024;
 constexpr uint32_t kDTmemCols = 256;
 
 template <bool BF16, typename OutT>
@@ -360,14 +430,18 @@ __global__ void __launch_bounds__(kDThreads, 2) tc_degridder_kernel(const TcArgs
     unsigned char *smem = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     unsigned char *bstat = smem;
     unsigned char *tiles = smem + kDStatic;
-    float *tab_m = reinterpret_cast<float *>(tiles + 2 * kDTileBytes);  // m[32], g[32]
+    unsigned char *ring = tiles + 2 * kDTileBytes;
+    float *tab_m = reinterpret_cast<float *>(ring + kDRing * kDRingSlot);  // m[32], g[32]
     float *tab_g = tab_m + kS;
     uint64_t *a_full = reinterpret_cast<uint64_t *>(tab_m + 2 * kS);
     uint64_t *a_empty = a_full + 2;
     uint64_t *acc_full = a_empty + 2;
     uint64_t *acc_empty = acc_full + 2;
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(acc_empty + 2);
+    uint64_t *in_full = acc_empty + 2;
+    uint64_t *in_empty = in_full + kDRing;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(in_empty + kDRing);
     volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
+    float *red = reinterpret_cast<float *>(tmem_slot + 2);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const Geometry &g = a.g;
@@ -375,7 +449,7 @@ __global__ void __launch_bounds__(kDThreads, 2) tc_degridder_kernel(const TcArgs
     const DevSubgrid sg = a.subs[it.subgrid];
     const int nvis = it.nt * g.nch;
     const int ntiles = (nvis + kDTile - 1) / kDTile;
-    const int64_t cbase = a.coef_off[it.subgrid] + static_cast<int64_t>(it.t0 - sg.t0) * g.nch;
+    const float4 *crow = a.coef + a.coef_off[it.subgrid] + static_cast<int64_t>(it.t0 - sg.t0) * g.nch;
 
     if (threadIdx.x == 0) {
         for (int b = 0; b < 2; b++) {
@@ -384,6 +458,10 @@ __global__ void __launch_bounds__(kDThreads, 2) tc_degridder_kernel(const TcArgs
             mbar_init(&acc_full[b], 1);
             mbar_init(&acc_empty[b], 4);
         }
+        for (int s = 0; s < kDRing; s++) {
+            mbar_init(&in_full[s], 32);  // one cp.async arrival per loader lane
+            mbar_init(&in_empty[s], 8);  // 4 producer + 4 epilogue warps read each slot
+        }
         *abort_flag = 0;
         mbar_fence_init();
     }
@@ -391,7 +469,7 @@ __global__ void __launch_bounds__(kDThreads, 2) tc_degridder_kernel(const TcArgs
         tab_m[threadIdx.x] = a.lmn[threadIdx.x];
         tab_g[threadIdx.x] = a.tabs[threadIdx.x];
     }
-    if (warp == 8) {
+    if (warp == kDMmaWarp) {
         tmem_alloc(tmem_slot, kDTmemCols);
         tmem_relinquish();
     }
@@ -407,7 +485,7 @@ __global__ void __launch_bounds__(kDThreads, 2) tc_degridder_kernel(const TcArgs
                 const float tap = fabsf(a.taper[pi]);
                 mx = fmaxf(mx, fmaxf(fabsf(d.x), fabsf(d.y)) * tap);
             }
-            sq = pow2_scale(block256_max(mx, reinterpret_cast<float *>(tmem_slot + 2)));
+            sq = pow2_scale(block256_max(mx, red));
         }
         const float sr = BF16 ? 1.f : a.r_scale;
         const uint32_t bs = smem_u32(bstat);
@@ -442,9 +520,9 @@ __global__ void __launch_bounds__(kDThreads, 2) tc_degridder_kernel(const TcArgs
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
-    const uint32_t bs = smem_u32(bstat), ts = smem_u32(tiles);
+    const uint32_t bs = smem_u32(bstat), ts = smem_u32(tiles), rbase = smem_u32(ring);
 
-    if (warp == 8) {
+    if (warp == kDMmaWarp) {
         // ---- MMA issuer
         if (lane == 0) {
             constexpr uint32_t id128 = idesc_f16(128, 128, BF16), id64 = idesc_f16(128, 64, BF16);
@@ -475,11 +553,60 @@ __global__ void __launch_bounds__(kDThreads, 2) tc_degridder_kernel(const TcArgs
             mma_commit(&a_empty[0]);
         }
         __syncwarp();
-    } else if (warp < 4) {
-        // ---- producers: A tile (128 visibilities x 32 x), hi and lo
+    } else if (warp == kDLoaderWarp) {
+        // ---- loader: tile i's 128 coefficients -> ring slot i % kDRing
         for (int i = 0; i < ntiles; i++) {
-            const int b = i & 1;
-            const uint32_t ph = (i >> 1) & 1;
+            const int slot = i % kDRing;
+            const uint32_t ph = (i / kDRing) & 1;
+            if (!warp_wait(&in_empty[slot], ph ^ 1, abort_flag, kWaitNs)) {
+                if (lane == 0) {
+                    *abort_flag = 1;
+                    atomicOr(a.status, kStatusWait);
+                }
+                break;
+            }
+            const uint32_t dst = rbase + slot * kDRingSlot;
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int row = lane + 32 * u, j = i * kDTile + row;
+                const bool in = j < nvis;
+                cp_async_16(dst + row * 16, in ? crow + j : crow, in ? 16u : 0u);
+            }
+            cp_async_arrive(&in_full[slot]);
+        }
+        asm volatile("cp.async.wait_all;" ::: "memory");
+    } else if (warp < 4) {
+        // ---- producers: A tile, hi and lo.  Thread t writes the 16-byte chunks cc = t + 128 u
+        // (u < 8): rows 8 (2u + t/64) + t%8 = row0 + 16 u, one fixed group of 4 x values.
+        const int kg = (threadIdx.x >> 3) & 7;
+        const int row0 = (threadIdx.x >> 6) * 8 + (threadIdx.x & 7);
+        float lx[4], fx[4];
+#pragma unroll
+        for (int v = 0; v < 4; v++) {
+            lx[v] = tab_m[kg * 4 + v];
+            fx[v] = tab_g[kg * 4 + v];
+        }
+        for (int i = 0; i < ntiles; i++) {
+            const int b = i & 1, slot = i % kDRing;
+            const uint32_t ph = (i >> 1) & 1, iph = (i / kDRing) & 1;
+            if (!warp_wait(&in_full[slot], iph, abort_flag, kWaitNs)) {
+                if (lane == 0) {
+                    *abort_flag = 1;
+                    atomicOr(a.status, kStatusWait);
+                }
+                break;
+            }
+            float2 cu[8];  // (du, dw) of this thread's 8 rows
+            {
+                const float4 *rc = reinterpret_cast<const float4 *>(ring + slot * kDRingSlot);
+#pragma unroll
+                for (int u = 0; u < 8; u++) {
+                    const float4 c = rc[row0 + 16 * u];
+                    cu[u] = make_float2(c.x, c.z);
+                }
+            }
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&in_empty[slot]);
             if (!warp_wait(&a_empty[b], ph ^ 1, abort_flag, kWaitNs)) {
                 if (lane == 0) {
                     *abort_flag = 1;
@@ -488,19 +615,14 @@ __global__ void __launch_bounds__(kDThreads, 2) tc_degridder_kernel(const TcArgs
                 break;
             }
             const uint32_t ahi = ts + b * kDTileBytes, alo = ahi + kDTileHalf;
+#pragma unroll
             for (int u = 0; u < 8; u++) {
                 const int cc = threadIdx.x + 128 * u;
-                const int cm = cc >> 3, r8 = cc & 7;
-                const int row = (cm >> 3) * 8 + r8, kg = cm & 7;
-                const int j = i * kDTile + row;
-                float4 c = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (j < nvis) c = a.coef[cbase + j];
                 uint32_t whi[4], wlo[4];
 #pragma unroll
                 for (int v = 0; v < 4; v++) {
-                    const int x = kg * 4 + v;
                     float sa, ca;
-                    __sincosf(fmaf(c.x, tab_m[x], c.z * tab_g[x]), &sa, &ca);
+                    __sincosf(fmaf(cu[u].x, lx[v], cu[u].y * fx[v]), &sa, &ca);
                     split_pair<BF16>(ca, sa, whi[v], wlo[v]);
                 }
                 st_shared_v4(ahi + cc * 16, whi[0], whi[1], whi[2], whi[3]);
@@ -513,10 +635,21 @@ __global__ void __launch_bounds__(kDThreads, 2) tc_degridder_kernel(const TcArgs
     } else {
         // ---- epilogue: one visibility per thread
         const int q = warp & 3;
-        OutT *out = static_cast<OutT *>(a.vis_out);
+        OutT *out = static_cast<OutT *>(a.vis_out) + (static_cast<int64_t>(sg.bl) * g.nt_all + it.t0) * g.nch;
         for (int i = 0; i < ntiles; i++) {
-            const int b = i & 1;
-            const uint32_t ph = (i >> 1) & 1;
+            const int b = i & 1, slot = i % kDRing;
+            const uint32_t ph = (i >> 1) & 1, iph = (i / kDRing) & 1;
+            const int row = q * 32 + lane, j = i * kDTile + row;
+            if (!warp_wait(&in_full[slot], iph, abort_flag, kWaitNs)) {
+                if (lane == 0) {
+                    *abort_flag = 1;
+                    atomicOr(a.status, kStatusWait);
+                }
+                break;
+            }
+            const float4 c = reinterpret_cast<const float4 *>(ring + slot * kDRingSlot)[row];
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&in_empty[slot]);
             if (!warp_wait(&acc_full[b], ph, abort_flag, kWaitNs)) {
                 if (lane == 0) {
                     *abort_flag = 1;
@@ -525,9 +658,6 @@ __global__ void __launch_bounds__(kDThreads, 2) tc_degridder_kernel(const TcArgs
                 break;
             }
             tc_fence_after();
-            const int j = i * kDTile + q * 32 + lane;
-            float4 c = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (j < nvis) c = a.coef[cbase + j];
             const float dwe = BF16 ? c.z : c.z / a.r_scale;  // T1 was formed from r * r_scale
             const uint32_t acc = tmem + (static_cast<uint32_t>(32 * q) << 16) + static_cast<uint32_t>(b * 128);
             float vre = 0.f, vim = 0.f;
@@ -553,16 +683,14 @@ __global__ void __launch_bounds__(kDThreads, 2) tc_degridder_kernel(const TcArgs
             __syncwarp();
             if (lane == 0) mbar_arrive(&acc_empty[b]);
             if (j < nvis) {
-                const int t = it.t0 + j / g.nch, ch = j - (j / g.nch) * g.nch;
                 const float sc = g.inv_s2 / sq;  // exact: sq is a power of two
-                store_vis(out, (static_cast<int64_t>(sg.bl) * g.nt_all + t) * g.nch + ch,
-                          make_float2(vre * sc, vim * sc));
+                store_vis(out, j, make_float2(vre * sc, vim * sc));
             }
         }
     }
     tc_fence_before();
     __syncthreads();
-    if (warp == 8) {
+    if (warp == kDMmaWarp) {
         // wait (bounded) for the drain commit: all MMAs of this CTA are complete
         if (lane == 0) {
             const int nb0 = (ntiles + 1) / 2;  // completed phases of a_empty[0] before the drain
@@ -709,10 +837,10 @@ p9idg_status tc_prepare(TcPlanState &st, const std::vector<p9idg_subgrid> &subs,
               std::to_string(st.max_w_r) + ")";
         return P9IDG_UNSUPPORTED;
     }
-    // degridder work items: whole time samples, up to 2048 visibilities each
+    // degridder work items: whole time samples, up to 4096 visibilities each
     std::vector<DevSubgrid> dtmp;
     std::vector<WorkItem> ditems;
-    build_work_items(subs, nch, 2048, dtmp, ditems);
+    build_work_items(subs, nch, 4096, dtmp, ditems);
     st.ncoef = off.back();
     cudaError_t e;
     if ((e = cudaMalloc(&st.coef, sizeof(float4) * std::max<int64_t>(1, st.ncoef))) != cudaSuccess ||
@@ -737,9 +865,11 @@ p9idg_status tc_prepare(TcPlanState &st, const std::vector<p9idg_subgrid> &subs,
     return P9IDG_OK;
 }
 
+// Per-visibility phase coefficients depend only on the plan and uvw: computed once and kept
+// until uvw is uploaded again (the plan clears coef_valid then).
 static p9idg_status launch_coef(TcPlanState &st, const GridderArgs &a, int32_t nsub, cudaStream_t stream,
                                 std::string &err) {
-    if (nsub == 0) return P9IDG_OK;
+    if (nsub == 0 || st.coef_valid) return P9IDG_OK;
     tc_coef_kernel<<<nsub, 256, 0, stream>>>(a.subs, static_cast<const int64_t *>(st.coef_off), a.uvw, a.wavenumbers,
                                              a.g, static_cast<float4 *>(st.coef));
     cudaError_t e = cudaGetLastError();
@@ -747,6 +877,7 @@ static p9idg_status launch_coef(TcPlanState &st, const GridderArgs &a, int32_t n
         err = std::string("coefficient kernel: ") + cudaGetErrorString(e);
         return P9IDG_CUDA_ERROR;
     }
+    st.coef_valid = true;
     return P9IDG_OK;
 }
 

@@ -11,6 +11,7 @@ namespace p9idg {
 // Per-plan state of the tensor-core kernels (device buffers and host-built tables).
 struct TcPlanState {
     bool ready = false;
+    bool coef_valid = false;      // coefficients match the uvw now on the device
     int S = 0;
     int64_t ncoef = 0;
     void *coef = nullptr;         // float4 {du, dv, dw, 0} per gridded visibility, subgrid order
