@@ -55,6 +55,16 @@ def _f64(a):
     return np.ascontiguousarray(a, dtype=np.float64)
 
 
+def _out(out, shape):
+    """A caller-supplied output array (checked) or a new one."""
+    if out is None:
+        return np.empty(shape, np.complex128)
+    if not (isinstance(out, np.ndarray) and out.dtype == np.complex128 and out.shape == tuple(shape)
+            and out.flags.c_contiguous and out.flags.writeable):
+        raise ValueError(f"out must be a writeable C-contiguous complex128 array of shape {tuple(shape)}")
+    return out
+
+
 class GriddingConstants:
     """Immutable gridding parameters (GriddingConstants.cs:11-52).
 
@@ -267,38 +277,40 @@ class IDG:
     """IDG.cs:10-115."""
 
     @staticmethod
-    def Grid(c, metadata, visibilities, uvw, frequencies) -> np.ndarray:
+    def Grid(c, metadata, visibilities, uvw, frequencies, out=None) -> np.ndarray:
         p = _plan_for(c, metadata, uvw, frequencies)
         vis, uvw = _c128(visibilities, "visibilities"), _f64(uvw)
-        out = np.empty((c.GridSize, c.GridSize), np.complex128)
+        out = _out(out, (c.GridSize, c.GridSize))
         _check(nat.lib().p9idg_grid(p.handle, _ptr(vis), _ptr(uvw), _ptr(out)))
         return out
 
     @staticmethod
-    def DeGrid(c, metadata, grid, uvw, frequencies) -> np.ndarray:
+    def DeGrid(c, metadata, grid, uvw, frequencies, out=None) -> np.ndarray:
         """Like the reference, FFT.Shift is applied to `grid` in place when it is a
         C-contiguous complex128 array."""
-        return IDG._degrid(c, metadata, grid, uvw, frequencies, nat.lib().p9idg_degrid)
+        return IDG._degrid(c, metadata, grid, uvw, frequencies, nat.lib().p9idg_degrid, out)
 
     @staticmethod
-    def GridW(c, metadata, visibilities, uvw, frequencies) -> np.ndarray:
+    def GridW(c, metadata, visibilities, uvw, frequencies, out=None) -> np.ndarray:
+        """`out` (optional): a C-contiguous complex128 [W][N][N] array to write into, e.g. in
+        page-locked memory; the reference returns a new List<Complex[,]>."""
         p = _plan_for(c, metadata, uvw, frequencies)
         vis, uvw = _c128(visibilities, "visibilities"), _f64(uvw)
-        out = np.empty((c.WLayerCount, c.GridSize, c.GridSize), np.complex128)
+        out = _out(out, (c.WLayerCount, c.GridSize, c.GridSize))
         _check(nat.lib().p9idg_grid_w(p.handle, _ptr(vis), _ptr(uvw), _ptr(out)))
         return out
 
     @staticmethod
-    def DeGridW(c, metadata, grid, uvw, frequencies) -> np.ndarray:
-        return IDG._degrid(c, metadata, grid, uvw, frequencies, nat.lib().p9idg_degrid_w)
+    def DeGridW(c, metadata, grid, uvw, frequencies, out=None) -> np.ndarray:
+        return IDG._degrid(c, metadata, grid, uvw, frequencies, nat.lib().p9idg_degrid_w, out)
 
     @staticmethod
-    def _degrid(c, metadata, grid, uvw, frequencies, fn):
+    def _degrid(c, metadata, grid, uvw, frequencies, fn, out=None):
         p = _plan_for(c, metadata, uvw, frequencies)
         g = grid if (isinstance(grid, np.ndarray) and grid.dtype == np.complex128 and grid.flags.c_contiguous
                      and grid.flags.writeable) else _c128(grid, "grid").copy()
         uvw = _f64(uvw)
-        vis = np.empty((p.nbl, p.nt, p.nch), np.complex128)
+        vis = _out(out, (p.nbl, p.nt, p.nch))
         _check(fn(p.handle, _ptr(g), _ptr(uvw), _ptr(vis)))
         return vis
 
