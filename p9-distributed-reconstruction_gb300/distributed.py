@@ -1,0 +1,97 @@
+"""Data-parallel gridding over baselines: the reference's MPI layout on torch.distributed.
+
+The reference shards the observation by contiguous baseline blocks
+(Distributed-Reference/DistributedData.cs:94-96), grids each block locally
+(MPIMajorCycle.cs:170, 208: IDG.Grid / IDG.GridPSF) and sums the N x N grids to rank 0
+with Reduce(SequentialSum) (MPIMajorCycle.cs:173, 209, 221-232), broadcasting images
+back (:106, 186-187, 215).  Here each rank partitions its own block (the partition is
+per baseline, so the subgrids are those of the global plan for these baselines), grids
+it on its GPU, and the grids (or w layers) are summed with one collective: NCCL on
+device tensors, or gloo on host arrays.  Gridding is linear in the visibilities, so the
+reduced grid equals the single-process grid up to summation order.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def baseline_block(nbl: int, world_size: int, rank: int) -> tuple[int, int]:
+    """[begin, end) baselines of `rank`: equal blocks, the last rank takes the remainder
+    (DistributedData.cs:94-96)."""
+    if world_size <= 0 or not (0 <= rank < world_size):
+        raise ValueError("invalid rank / world size")
+    per = int(nbl / world_size)
+    begin = rank * per
+    end = (rank + 1) * per if rank + 1 < world_size else nbl
+    return begin, end
+
+
+def local_block(arrays, nbl, world_size, rank):
+    """Slices this rank's baselines out of [nbl, ...] arrays (uvw, visibilities, flags)."""
+    b, e = baseline_block(nbl, world_size, rank)
+    return [None if a is None else np.ascontiguousarray(a[b:e]) for a in arrays]
+
+
+def _as_real_tensor(torch, arr):
+    """A float64/float32 torch view of a complex numpy array (collectives sum real pairs)."""
+    a = np.ascontiguousarray(arr)
+    if np.iscomplexobj(a):
+        a = a.view(np.float64 if a.dtype == np.complex128 else np.float32)
+    return torch.from_numpy(a)
+
+
+class GridReducer:
+    """Sums grids across ranks (Reduce(SequentialSum) of MPIMajorCycle.cs:221-232)."""
+
+    def __init__(self, group=None):
+        import torch
+        import torch.distributed as dist
+
+        self.torch = torch
+        self.dist = dist
+        self.group = group
+        self.rank = dist.get_rank(group)
+        self.world_size = dist.get_world_size(group)
+
+    def sum_to_root(self, grid: np.ndarray, root: int = 0):
+        """Host array (complex or real): the element-wise sum lands on `root` (None elsewhere)."""
+        t = _as_real_tensor(self.torch, grid).clone()
+        self.dist.reduce(t, dst=root, op=self.dist.ReduceOp.SUM, group=self.group)
+        if self.rank != root:
+            return None
+        out = t.numpy()
+        return out.view(grid.dtype).reshape(grid.shape) if np.iscomplexobj(grid) else out.reshape(grid.shape)
+
+    def sum_all(self, grid: np.ndarray) -> np.ndarray:
+        t = _as_real_tensor(self.torch, grid).clone()
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.SUM, group=self.group)
+        out = t.numpy()
+        return out.view(grid.dtype).reshape(grid.shape) if np.iscomplexobj(grid) else out.reshape(grid.shape)
+
+    def sum_device_(self, tensor):
+        """In-place all-reduce of a device tensor (complex64 grids are summed as float pairs)."""
+        t = self.torch.view_as_real(tensor) if tensor.is_complex() else tensor
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.SUM, group=self.group)
+        return tensor
+
+    def broadcast(self, arr, root: int = 0):
+        """Host array from `root` to every rank (MPIMajorCycle.cs:106, 186-187, 215)."""
+        t = _as_real_tensor(self.torch, arr).clone()
+        self.dist.broadcast(t, src=root, group=self.group)
+        out = t.numpy()
+        return out.view(arr.dtype).reshape(arr.shape) if np.iscomplexobj(arr) else out.reshape(arr.shape)
+
+
+def distributed_grid(reducer: GridReducer, c, uvw_all, vis_all, frequencies, gridder, root: int = 0,
+                     partitioner=None):
+    """ForwardCalculateB's gridding half (MPIMajorCycle.cs:160-174): partition and grid this
+    rank's baseline block with `gridder(c, partition, vis, uvw, freq)`, then sum to `root`.
+
+    `partitioner(c, uvw, freq)` defaults to Partitioner.CreatePartition of this package."""
+    uvw, vis = local_block([uvw_all, vis_all], uvw_all.shape[0], reducer.world_size, reducer.rank)
+    if partitioner is None:
+        from .idg import Partitioner
+        partitioner = Partitioner.CreatePartition
+    part = partitioner(c, uvw, frequencies)
+    local = gridder(c, part, vis, uvw, frequencies)
+    return reducer.sum_to_root(np.ascontiguousarray(local), root)
