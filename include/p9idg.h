@@ -184,6 +184,48 @@ p9idg_status p9idg_grid_w_device_noalloc(const p9idg_params *c, const p9idg_subg
                                          const double *d_uvw, int32_t nbl, int32_t nt, const double *frequencies,
                                          int32_t nch, const void *d_vis, void *d_layers, void *cuda_stream);
 
+/* ---------------- batches of independent problems (no counterpart in the reference) ---------------- */
+/* Many plans (imaging problems of different sizes) gridded and degridded together: every
+ * kernel stage is ONE launch over the work items of all problems, ordered largest first, so
+ * small problems fill the GPU alongside large ones.  Buffers are the per-problem device
+ * buffers of p9idg_grid_w_device / p9idg_degrid_w_device (complex64), fixed at creation.
+ * All plans must share the precision mode and the subgrid size. */
+typedef struct p9idg_batch p9idg_batch;
+
+/* Work-item sizes (visibilities per gridder / degridder item; 0 = default) -- the time-chunk
+ * length the autotuner chooses. */
+p9idg_status p9idg_plan_set_chunking(p9idg_plan *plan, int32_t gridder_max_vis, int32_t degridder_max_vis);
+p9idg_status p9idg_batch_create(p9idg_plan *const *plans, int32_t nplans, const void *const *d_vis,
+                                void *const *d_layers, const void *const *d_grids, void *const *d_vis_out,
+                                p9idg_batch **out);
+/* IDG.GridW / IDG.DeGridW for every problem of the batch (asynchronous, on the batch's stream). */
+p9idg_status p9idg_batch_grid_w(p9idg_batch *batch);
+p9idg_status p9idg_batch_degrid_w(p9idg_batch *batch);
+/* Records grid_w + degrid_w into a CUDA graph; later p9idg_batch_run calls replay it. */
+p9idg_status p9idg_batch_capture_graph(p9idg_batch *batch);
+/* grid_w then degrid_w (graph replay once captured). */
+p9idg_status p9idg_batch_run(p9idg_batch *batch);
+p9idg_status p9idg_batch_synchronize(p9idg_batch *batch);
+/* Per problem: ms from the start of the last degrid phase to the problem's last visibility (-1 if none). */
+p9idg_status p9idg_batch_latencies(p9idg_batch *batch, double *ms);
+p9idg_status p9idg_batch_get_stream(const p9idg_batch *batch, void **cuda_stream);
+void p9idg_batch_destroy(p9idg_batch *batch);
+
+/* Autotuner: times grid + degrid on a sample of the observation's baselines for each candidate
+ * subgrid size (and work-item size) and returns the fastest per gridded visibility among the
+ * candidates that drop no more visibilities than the best of them. */
+typedef struct p9idg_tuning {
+    int32_t subgrid_size;
+    int32_t kernel_size;
+    int32_t gridder_max_vis;
+    int32_t degridder_max_vis;
+    double seconds_per_gridded_vis;  /* grid + degrid, measured on the sample */
+    double gridded_fraction;         /* of the sample's visibilities */
+} p9idg_tuning;
+p9idg_status p9idg_autotune(const p9idg_params *c, const double *uvw, int32_t nbl, int32_t nt,
+                            const double *frequencies, int32_t nch, int32_t mode, const int32_t *subgrid_sizes,
+                            int32_t nsizes, p9idg_tuning *out);
+
 /* ---------------- stage timing (CUDA events on the plan's stream) ---------------- */
 
 enum {

@@ -7,9 +7,9 @@ mirror of the reference API over that ABI.
 """
 from . import _native
 from ._native import (MODE_FP32, MODE_TC_BF16X3, MODE_TC_FP16X3, NativeLibraryMissing, STAGES)
-from .idg import (FFT, IDG, GriddingConstants, P9IDGError, Partition, Partitioner, Plan, Subgrid, SUBGRID_DTYPE,
-                  device_count, measure_sincos_peak, plan_from_subgrids)
+from .idg import (FFT, IDG, Batch, GriddingConstants, P9IDGError, Partition, Partitioner, Plan, Subgrid, SUBGRID_DTYPE,
+                  autotune, device_count, measure_sincos_peak, plan_from_subgrids, set_chunking)
 
-__all__ = ["FFT", "IDG", "GriddingConstants", "P9IDGError", "Partition", "Partitioner", "Plan", "Subgrid",
+__all__ = ["FFT", "IDG", "Batch", "autotune", "set_chunking", "GriddingConstants", "P9IDGError", "Partition", "Partitioner", "Plan", "Subgrid",
            "SUBGRID_DTYPE", "MODE_FP32", "MODE_TC_BF16X3", "MODE_TC_FP16X3", "NativeLibraryMissing", "STAGES",
            "device_count", "measure_sincos_peak", "plan_from_subgrids"]

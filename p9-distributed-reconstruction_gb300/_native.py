@@ -91,6 +91,18 @@ SIGNATURES = {
     "p9idg_device_count": (i32, []),
     "p9idg_measure_sincos_peak": (i32, [ctypes.POINTER(dbl), ctypes.POINTER(dbl)]),
     "p9idg_tc_selftest": (i32, [i32, i32, ctypes.POINTER(dbl)]),
+    "p9idg_plan_set_chunking": (i32, [P, i32, i32]),
+    "p9idg_batch_create": (i32, [ctypes.POINTER(P), i32, ctypes.POINTER(P), ctypes.POINTER(P), ctypes.POINTER(P),
+                                 ctypes.POINTER(P), ctypes.POINTER(P)]),
+    "p9idg_batch_grid_w": (i32, [P]),
+    "p9idg_batch_degrid_w": (i32, [P]),
+    "p9idg_batch_capture_graph": (i32, [P]),
+    "p9idg_batch_run": (i32, [P]),
+    "p9idg_batch_synchronize": (i32, [P]),
+    "p9idg_batch_latencies": (i32, [P, P]),
+    "p9idg_batch_get_stream": (i32, [P, ctypes.POINTER(P)]),
+    "p9idg_batch_destroy": (None, [P]),
+    "p9idg_autotune": (i32, [P, P, i32, i32, P, i32, i32, P, i32, P]),
 }
 
 _lib = None

@@ -119,6 +119,8 @@ struct p9idg_plan {
     std::vector<WorkItem> gitems, ditems;
     int32_t nslots = 0;
     bool items_dirty = true;  // gridder items / subgrid list not yet on the device
+    int32_t gchunk = 0;       // gridder visibilities per work item (0 = per-mode default)
+    int32_t dchunk = 0;       // degridder visibilities per work item (0 = per-mode default)
     int64_t gridded_vis = 0;
     std::vector<float> lmn, taper;
     std::vector<float> add_phasor;  // interleaved float2 [S][S]
@@ -216,7 +218,11 @@ p9idg_status check_params(const p9idg_params *c) {
 // 4096 for the tensor-core kernel (its per-item epilogue is heavier).  The subgrid list
 // records each subgrid's item slots for the subgrid IFFT + adder.
 void build_gridder_items(p9idg_plan *p) {
-    build_work_items(p->subs, p->nch, p->mode == P9IDG_MODE_FP32 ? 1024 : 4096, p->dsub, p->gitems);
+    const int64_t chunk = p->gchunk > 0 ? p->gchunk : (p->mode == P9IDG_MODE_FP32 ? 1024 : 4096);
+    build_work_items(p->subs, p->nch, chunk, p->dsub, p->gitems);
+    // FP32 degridder items: 512 visibilities by default (4 per thread of a 128-thread block)
+    std::vector<DevSubgrid> tmp;
+    build_work_items(p->subs, p->nch, p->dchunk > 0 ? p->dchunk : 512, tmp, p->ditems);
     p->nslots = 0;
     for (const auto &d : p->dsub) p->nslots += d.item_count;
     p->items_dirty = true;
@@ -224,10 +230,7 @@ void build_gridder_items(p9idg_plan *p) {
 
 void finish_plan(p9idg_plan *p) {
     const int S = p->c.subgrid_size;
-    // degridder items: up to 512 visibilities (4 per thread of a 128-thread block)
-    std::vector<DevSubgrid> tmp;
     build_gridder_items(p);
-    build_work_items(p->subs, p->nch, 512, tmp, p->ditems);
     p->gridded_vis = 0;
     for (const auto &s : p->subs) p->gridded_vis += static_cast<int64_t>(s.time_sample_count) * p->nch;
     const float img = image_size(p->c);
@@ -262,16 +265,12 @@ p9idg_status ensure_device(p9idg_plan *p) {
     if (!p->stream) p->stream = p->own_stream;
     const int S = p->c.subgrid_size;
     CK(p->d_wn.ensure(sizeof(double) * std::max(1, p->nch)));
-    CK(p->d_ditems.ensure(sizeof(WorkItem) * std::max<size_t>(1, p->ditems.size())));
     CK(p->d_lmn.ensure(sizeof(float) * p->lmn.size()));
     CK(p->d_taper.ensure(sizeof(float) * S * S));
     CK(p->d_phasor.ensure(sizeof(float) * 2 * S * S));
     CK(p->d_status.ensure(sizeof(int32_t)));
     cudaStream_t st = p->stream;
     CK(cudaMemcpyAsync(p->d_wn.p, p->wn.data(), sizeof(double) * p->nch, cudaMemcpyHostToDevice, st));
-    if (!p->ditems.empty())
-        CK(cudaMemcpyAsync(p->d_ditems.p, p->ditems.data(), sizeof(WorkItem) * p->ditems.size(),
-                           cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(p->d_lmn.p, p->lmn.data(), sizeof(float) * p->lmn.size(), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(p->d_phasor.p, p->add_phasor.data(), sizeof(float) * p->add_phasor.size(),
                        cudaMemcpyHostToDevice, st));
@@ -302,6 +301,10 @@ p9idg_status upload_uvw(p9idg_plan *p, const double *uvw) {
 p9idg_status upload_items(p9idg_plan *p) {
     CK(p->d_sub.ensure(sizeof(DevSubgrid) * std::max<size_t>(1, p->dsub.size())));
     CK(p->d_gitems.ensure(sizeof(WorkItem) * std::max<size_t>(1, p->gitems.size())));
+    CK(p->d_ditems.ensure(sizeof(WorkItem) * std::max<size_t>(1, p->ditems.size())));
+    if (!p->ditems.empty())
+        CK(cudaMemcpyAsync(p->d_ditems.p, p->ditems.data(), sizeof(WorkItem) * p->ditems.size(),
+                           cudaMemcpyHostToDevice, p->stream));
     if (!p->dsub.empty())
         CK(cudaMemcpyAsync(p->d_sub.p, p->dsub.data(), sizeof(DevSubgrid) * p->dsub.size(), cudaMemcpyHostToDevice,
                            p->stream));
@@ -350,6 +353,7 @@ GridderArgs gridder_args(p9idg_plan *p) {
 
 p9idg_status ensure_tc(p9idg_plan *p) {
     if (p->tc.ready) return P9IDG_OK;
+    p->tc.degrid_chunk = p->dchunk > 0 ? p->dchunk : 4096;
     return tc_prepare(p->tc, p->subs, p->lmn, p->c.subgrid_size, p->nch, p->wn, p->uvw.data(), p->nt, p->stream,
                       g_last_error);
 }
@@ -570,6 +574,93 @@ struct Standalone {
 Standalone &standalone() {
     static Standalone s;
     return s;
+}
+
+}  // namespace
+
+// ---------- batches: many plans, one launch per kernel stage ----------
+
+struct p9idg_batch {
+    std::vector<p9idg_plan *> plans;
+    int device = -1;
+    int32_t mode = P9IDG_MODE_FP32;
+    int32_t S = 0;
+    cudaStream_t stream = nullptr;
+    DevBuf d_gargs, d_dargs, d_aargs, d_sargs, d_tg, d_td;  // per-problem argument tables
+    DevBuf d_gitems, d_ditems, d_refs, d_done_init, d_done, d_finish, d_start;
+    int32_t ngitems = 0, nditems = 0, nrefs = 0;
+    std::vector<void *> layers, vis_out;
+    std::vector<size_t> layer_bytes, vis_bytes;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
+namespace {
+
+__global__ void stamp_kernel(unsigned long long *t) { *t = device_ns(); }
+
+p9idg_status batch_grid(p9idg_batch *b) {
+    for (size_t i = 0; i < b->plans.size(); i++)
+        CK(cudaMemsetAsync(b->layers[i], 0, b->layer_bytes[i], b->stream));
+    GridderArgs L{};
+    L.g.S = b->S;
+    L.items = b->d_gitems.as<WorkItem>();
+    L.nitems = b->ngitems;
+    if (b->mode == P9IDG_MODE_FP32) {
+        CK(launch_gridder_fp32(L, b->stream, b->d_gargs.as<GridderArgs>()));
+    } else {
+        TRY(tc_grid_batch(b->d_tg.as<TcArgs>(), b->d_gitems.as<WorkItem>(), b->ngitems, b->mode, b->stream,
+                          g_last_error));
+    }
+    SubgridOpArgs A{};
+    A.g.S = b->S;
+    A.refs = b->d_refs.as<int2>();
+    A.nsub = b->nrefs;
+    A.wstack = true;
+    CK(launch_subgrid_ifft_add(A, b->stream, b->d_aargs.as<SubgridOpArgs>()));
+    return P9IDG_OK;
+}
+
+p9idg_status batch_degrid(p9idg_batch *b) {
+    const size_t n = b->plans.size();
+    stamp_kernel<<<1, 1, 0, b->stream>>>(b->d_start.as<unsigned long long>());
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(b->d_done.p, b->d_done_init.p, sizeof(int32_t) * n, cudaMemcpyDeviceToDevice, b->stream));
+    CK(cudaMemsetAsync(b->d_finish.p, 0, sizeof(unsigned long long) * n, b->stream));
+    SubgridOpArgs A{};
+    A.g.S = b->S;
+    A.refs = b->d_refs.as<int2>();
+    A.nsub = b->nrefs;
+    A.wstack = true;
+    CK(launch_split_subgrid_fft(A, b->stream, b->d_sargs.as<SubgridOpArgs>()));
+    for (size_t i = 0; i < n; i++) CK(cudaMemsetAsync(b->vis_out[i], 0, b->vis_bytes[i], b->stream));
+    GridderArgs L{};
+    L.g.S = b->S;
+    L.items = b->d_ditems.as<WorkItem>();
+    L.nitems = b->nditems;
+    if (b->mode == P9IDG_MODE_FP32) {
+        CK(launch_degridder_fp32(L, b->stream, b->d_dargs.as<GridderArgs>()));
+    } else {
+        TRY(tc_degrid_batch(b->d_td.as<TcArgs>(), b->d_ditems.as<WorkItem>(), b->nditems, b->mode, b->stream,
+                            g_last_error));
+    }
+    return P9IDG_OK;
+}
+
+template <typename T>
+p9idg_status upload(DevBuf &buf, const std::vector<T> &v) {
+    CK(buf.ensure(sizeof(T) * std::max<size_t>(1, v.size())));
+    if (!v.empty()) CK(cudaMemcpy(buf.p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice));
+    return P9IDG_OK;
+}
+
+void batch_release(p9idg_batch *b) {
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    DevBuf *bufs[] = {&b->d_gargs, &b->d_dargs, &b->d_aargs, &b->d_sargs, &b->d_tg, &b->d_td, &b->d_gitems,
+                      &b->d_ditems, &b->d_refs, &b->d_done_init, &b->d_done, &b->d_finish, &b->d_start};
+    for (DevBuf *x : bufs) x->release();
+    if (b->stream) cudaStreamDestroy(b->stream);
 }
 
 }  // namespace
@@ -961,6 +1052,220 @@ p9idg_status p9idg_measure_sincos_peak(double *sincos_per_s, double *fma_per_s) 
     if (p9idg_device_count() == 0) return fail(P9IDG_NO_DEVICE, "no CUDA device available");
     CK(measure_sincos(sincos_per_s, fma_per_s));
     return P9IDG_OK;
+}
+
+// ---- work-item sizes and batches ----
+
+p9idg_status p9idg_plan_set_chunking(p9idg_plan *plan, int32_t gridder_max_vis, int32_t degridder_max_vis) {
+    if (!plan || gridder_max_vis < 0 || degridder_max_vis < 0) return fail(P9IDG_INVALID_ARGUMENT, "invalid argument");
+    plan->gchunk = gridder_max_vis;
+    plan->dchunk = degridder_max_vis;
+    build_gridder_items(plan);
+    if (plan->tc.ready) {
+        if (plan->dev_ready) {
+            CK(cudaSetDevice(plan->device));
+            CK(cudaStreamSynchronize(plan->stream));
+        }
+        tc_release(plan->tc);  // rebuilt (with the new degridder items) on the next tensor-core call
+    }
+    return P9IDG_OK;
+}
+
+p9idg_status p9idg_batch_create(p9idg_plan *const *plans, int32_t nplans, const void *const *d_vis,
+                                void *const *d_layers, const void *const *d_grids, void *const *d_vis_out,
+                                p9idg_batch **out) {
+    if (!out || !plans || nplans <= 0 || !d_vis || !d_layers || !d_grids || !d_vis_out)
+        return fail(P9IDG_INVALID_ARGUMENT, "invalid argument");
+    *out = nullptr;
+    for (int i = 0; i < nplans; i++) {
+        if (!plans[i] || !d_vis[i] || !d_layers[i] || !d_grids[i] || !d_vis_out[i])
+            return fail(P9IDG_INVALID_ARGUMENT, "null plan or buffer");
+        if (plans[i]->mode != plans[0]->mode || plans[i]->c.subgrid_size != plans[0]->c.subgrid_size)
+            return fail(P9IDG_UNSUPPORTED, "a batch needs one precision mode and one subgrid size");
+    }
+    auto *b = new (std::nothrow) p9idg_batch();
+    if (!b) return fail(P9IDG_OUT_OF_MEMORY, "batch allocation");
+    auto bail = [&](p9idg_status st) {
+        batch_release(b);
+        delete b;
+        return st;
+    };
+    b->plans.assign(plans, plans + nplans);
+    b->mode = plans[0]->mode;
+    b->S = plans[0]->c.subgrid_size;
+    const int S = b->S;
+    std::vector<GridderArgs> ga(nplans), da(nplans);
+    std::vector<SubgridOpArgs> aa(nplans), sa(nplans);
+    std::vector<TcArgs> tg(nplans), td(nplans);
+    std::vector<WorkItem> gitems, ditems;
+    std::vector<int2> refs;
+    std::vector<int32_t> done(nplans, 0);
+    // device-side completion tracking first: the argument tables point into it
+    p9idg_status st;
+    for (int i = 0; i < nplans; i++) {
+        p9idg_plan *p = plans[i];
+        if ((st = check_wstack_layers(p)) != P9IDG_OK) return bail(st);
+        if ((st = prepare(p, nullptr)) != P9IDG_OK) return bail(st);
+        if (i == 0) b->device = p->device;
+        if (p->device != b->device) return bail(fail(P9IDG_UNSUPPORTED, "a batch runs on one device"));
+    }
+    {
+        cudaError_t e = cudaSetDevice(b->device);
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = b->d_done.ensure(sizeof(int32_t) * nplans);
+        if (e == cudaSuccess) e = b->d_done_init.ensure(sizeof(int32_t) * nplans);
+        if (e == cudaSuccess) e = b->d_finish.ensure(sizeof(unsigned long long) * nplans);
+        if (e == cudaSuccess) e = b->d_start.ensure(sizeof(unsigned long long));
+        if (e != cudaSuccess) return bail(cuda_fail(e, "batch buffers"));
+    }
+    for (int i = 0; i < nplans; i++) {
+        p9idg_plan *p = plans[i];
+        cudaError_t e = p->d_partials.ensure(sizeof(float2) * S * S * std::max<size_t>(1, p->nslots));
+        if (e == cudaSuccess) e = p->d_subgrids.ensure(sizeof(float2) * S * S * std::max<size_t>(1, p->dsub.size()));
+        if (e != cudaSuccess) return bail(cuda_fail(e, "plan buffers"));
+        ga[i] = gridder_args(p);
+        ga[i].vis = d_vis[i];
+        ga[i].vis_c128 = false;
+        ga[i].partials = p->d_partials.as<float2>();
+        da[i] = gridder_args(p);
+        da[i].subgrids = p->d_subgrids.as<float2>();
+        da[i].vis_out = d_vis_out[i];
+        da[i].out_c128 = false;
+        da[i].done = b->d_done.as<int32_t>() + i;
+        da[i].finish_ns = b->d_finish.as<unsigned long long>() + i;
+        aa[i] = subgrid_args(p);
+        aa[i].partials = p->d_partials.as<float2>();
+        aa[i].layers = static_cast<float2 *>(d_layers[i]);
+        aa[i].out_shifted = true;
+        aa[i].wstack = true;
+        sa[i] = subgrid_args(p);
+        sa[i].grid = static_cast<const float2 *>(d_grids[i]);
+        sa[i].grid_shifted = false;
+        sa[i].subgrids = p->d_subgrids.as<float2>();
+        sa[i].wstack = true;
+        const std::vector<WorkItem> *dsrc = &p->ditems;
+        if (b->mode != P9IDG_MODE_FP32) {
+            if ((st = ensure_tc(p)) != P9IDG_OK) return bail(st);
+            if ((st = tc_coefs(p->tc, ga[i], p->stream, g_last_error)) != P9IDG_OK) return bail(st);
+            tc_fill_args(p->tc, ga[i], tg[i]);
+            tc_fill_args(p->tc, da[i], td[i]);
+            dsrc = &p->tc.ditems_host;
+        }
+        for (WorkItem w : p->gitems) {
+            w.problem = i;
+            gitems.push_back(w);
+        }
+        for (WorkItem w : *dsrc) {
+            w.problem = i;
+            ditems.push_back(w);
+        }
+        done[i] = static_cast<int32_t>(dsrc->size());
+        for (size_t s = 0; s < p->dsub.size(); s++) refs.push_back(make_int2(i, static_cast<int>(s)));
+        b->layers.push_back(d_layers[i]);
+        b->layer_bytes.push_back(sizeof(float2) * static_cast<size_t>(p->c.wlayer_count) * nn_of(p));
+        b->vis_out.push_back(d_vis_out[i]);
+        b->vis_bytes.push_back(sizeof(float2) * vis_count_of(p));
+        cudaError_t e2 = cudaStreamSynchronize(p->stream);
+        if (e2 != cudaSuccess) return bail(cuda_fail(e2, "plan preparation"));
+    }
+    // one largest-first schedule across every problem
+    auto by_size = [&](const WorkItem &x, const WorkItem &y) {
+        return static_cast<int64_t>(x.nt) * plans[x.problem]->nch > static_cast<int64_t>(y.nt) * plans[y.problem]->nch;
+    };
+    std::stable_sort(gitems.begin(), gitems.end(), by_size);
+    std::stable_sort(ditems.begin(), ditems.end(), by_size);
+    b->ngitems = static_cast<int32_t>(gitems.size());
+    b->nditems = static_cast<int32_t>(ditems.size());
+    b->nrefs = static_cast<int32_t>(refs.size());
+    if ((st = upload(b->d_gargs, ga)) != P9IDG_OK || (st = upload(b->d_dargs, da)) != P9IDG_OK ||
+        (st = upload(b->d_aargs, aa)) != P9IDG_OK || (st = upload(b->d_sargs, sa)) != P9IDG_OK ||
+        (st = upload(b->d_tg, tg)) != P9IDG_OK || (st = upload(b->d_td, td)) != P9IDG_OK ||
+        (st = upload(b->d_gitems, gitems)) != P9IDG_OK || (st = upload(b->d_ditems, ditems)) != P9IDG_OK ||
+        (st = upload(b->d_refs, refs)) != P9IDG_OK || (st = upload(b->d_done_init, done)) != P9IDG_OK)
+        return bail(st);
+    *out = b;
+    return P9IDG_OK;
+}
+
+p9idg_status p9idg_batch_grid_w(p9idg_batch *b) {
+    if (!b) return fail(P9IDG_INVALID_ARGUMENT, "null batch");
+    CK(cudaSetDevice(b->device));
+    return batch_grid(b);
+}
+
+p9idg_status p9idg_batch_degrid_w(p9idg_batch *b) {
+    if (!b) return fail(P9IDG_INVALID_ARGUMENT, "null batch");
+    CK(cudaSetDevice(b->device));
+    return batch_degrid(b);
+}
+
+p9idg_status p9idg_batch_run(p9idg_batch *b) {
+    if (!b) return fail(P9IDG_INVALID_ARGUMENT, "null batch");
+    CK(cudaSetDevice(b->device));
+    if (b->exec) {
+        CK(cudaGraphLaunch(b->exec, b->stream));
+        return P9IDG_OK;
+    }
+    TRY(batch_grid(b));
+    return batch_degrid(b);
+}
+
+p9idg_status p9idg_batch_capture_graph(p9idg_batch *b) {
+    if (!b) return fail(P9IDG_INVALID_ARGUMENT, "null batch");
+    CK(cudaSetDevice(b->device));
+    if (b->exec) return P9IDG_OK;
+    // one eager pass first: module loading and kernel attributes happen outside the capture
+    TRY(batch_grid(b));
+    TRY(batch_degrid(b));
+    CK(cudaStreamSynchronize(b->stream));
+    CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+    p9idg_status st = batch_grid(b);
+    if (st == P9IDG_OK) st = batch_degrid(b);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+    if (st != P9IDG_OK) {
+        if (g) cudaGraphDestroy(g);
+        return st;
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+    b->graph = g;
+    CK(cudaGraphInstantiate(&b->exec, b->graph, 0));
+    return P9IDG_OK;
+}
+
+p9idg_status p9idg_batch_synchronize(p9idg_batch *b) {
+    if (!b) return fail(P9IDG_INVALID_ARGUMENT, "null batch");
+    CK(cudaSetDevice(b->device));
+    CK(cudaStreamSynchronize(b->stream));
+    for (p9idg_plan *p : b->plans) TRY(finish_call(p));
+    return P9IDG_OK;
+}
+
+p9idg_status p9idg_batch_latencies(p9idg_batch *b, double *ms) {
+    if (!b || !ms) return fail(P9IDG_INVALID_ARGUMENT, "null argument");
+    CK(cudaSetDevice(b->device));
+    CK(cudaStreamSynchronize(b->stream));
+    const size_t n = b->plans.size();
+    std::vector<unsigned long long> fin(n);
+    unsigned long long start = 0;
+    CK(cudaMemcpy(fin.data(), b->d_finish.p, sizeof(unsigned long long) * n, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(&start, b->d_start.p, sizeof(start), cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < n; i++) ms[i] = fin[i] >= start ? static_cast<double>(fin[i] - start) * 1e-6 : -1.0;
+    return P9IDG_OK;
+}
+
+p9idg_status p9idg_batch_get_stream(const p9idg_batch *b, void **cuda_stream) {
+    if (!b || !cuda_stream) return fail(P9IDG_INVALID_ARGUMENT, "null argument");
+    *cuda_stream = b->stream;
+    return P9IDG_OK;
+}
+
+void p9idg_batch_destroy(p9idg_batch *b) {
+    if (!b) return;
+    cudaSetDevice(b->device);
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    batch_release(b);
+    delete b;
 }
 
 }  // extern "C"

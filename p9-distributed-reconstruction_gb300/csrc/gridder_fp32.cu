@@ -12,7 +12,8 @@
 //
 // Work is split into (subgrid, time chunk) items ordered largest first.  The gridder
 // writes one partial subgrid per item (summed, in a fixed order, by the subgrid IFFT
-// kernel), so results do not depend on scheduling.
+// kernel), so results do not depend on scheduling.  Batched launches cover the items of
+// many problems (plans); each item then reads its problem's arguments from a table.
 
 #include "kernels.cuh"
 
@@ -31,15 +32,17 @@ __host__ __device__ constexpr int ppt_for(int S) {
 constexpr int kDegridThreads = 128;
 constexpr int kDegridVpt = 4;  // visibilities per degridder thread
 
-template <int S, typename VisT>
-__global__ void __launch_bounds__(S * S / ppt_for(S)) gridder_fp32_kernel(const GridderArgs a) {
+template <int S, typename VisT, bool BATCH>
+__global__ void __launch_bounds__(S * S / ppt_for(S))
+    gridder_fp32_kernel(const GridderArgs L, const GridderArgs *__restrict__ probs) {
     constexpr int PPT = ppt_for(S);
     constexpr int NT = S * S / PPT;
     __shared__ float4 s_d[NT];  // per-visibility phase coefficients (du, dv, dw)
     __shared__ float2 s_v[NT];  // visibilities
 
-    const Geometry &g = a.g;
-    const WorkItem it = a.items[blockIdx.x];
+    const WorkItem it = L.items[blockIdx.x];
+    const GridderArgs &a = BATCH ? probs[it.problem] : L;
+    const Geometry g = a.g;
     const DevSubgrid sg = a.subs[it.subgrid];
     const int tid = threadIdx.x;
     const int p0 = tid * PPT;
@@ -59,14 +62,16 @@ __global__ void __launch_bounds__(S * S / ppt_for(S)) gridder_fp32_kernel(const 
     const double woff = 2 * kPi * (static_cast<double>(g.wstep_lambda) * (static_cast<double>(sg.w) + 0.5));
 
     const VisT *vis = static_cast<const VisT *>(a.vis);
+    const double *uvw = a.uvw;
+    const double *wn = a.wavenumbers;
     const int nvis = it.nt * g.nch;
     for (int b = 0; b < nvis; b += NT) {
         const int j = b + tid;
         if (j < nvis) {
             const int t = it.t0 + j / g.nch, ch = j - (j / g.nch) * g.nch;
             const int64_t row = static_cast<int64_t>(sg.bl) * g.nt_all + t;
-            const double *q = a.uvw + row * 3;
-            const double k = a.wavenumbers[ch];
+            const double *q = uvw + row * 3;
+            const double k = wn[ch];
             const double du = uoff - k * q[0];
             const double dv = voff - k * q[1];
             const double dw = woff - k * q[2];
@@ -102,13 +107,15 @@ __global__ void __launch_bounds__(S * S / ppt_for(S)) gridder_fp32_kernel(const 
     }
 }
 
-template <int S, typename OutT>
-__global__ void __launch_bounds__(kDegridThreads) degridder_fp32_kernel(const GridderArgs a) {
+template <int S, typename OutT, bool BATCH>
+__global__ void __launch_bounds__(kDegridThreads)
+    degridder_fp32_kernel(const GridderArgs L, const GridderArgs *__restrict__ probs) {
     extern __shared__ float4 s_pix[];  // [S*S] {re, im, l_x, n_xy}, tapered and un-shifted
     __shared__ float s_m[S];
 
-    const Geometry &g = a.g;
-    const WorkItem it = a.items[blockIdx.x];
+    const WorkItem it = L.items[blockIdx.x];
+    const GridderArgs &a = BATCH ? probs[it.problem] : L;
+    const Geometry g = a.g;
     const DevSubgrid sg = a.subs[it.subgrid];
     const int tid = threadIdx.x;
     const float2 *data = a.subgrids + static_cast<int64_t>(it.subgrid) * S * S;
@@ -126,6 +133,8 @@ __global__ void __launch_bounds__(kDegridThreads) degridder_fp32_kernel(const Gr
     const double voff = static_cast<double>(sg.v + S / 2 - g.N / 2) * g.uv_scale;
     const double woff = 2 * kPi * (static_cast<double>(g.wstep_lambda) * (static_cast<double>(sg.w) + 0.5));
     OutT *out = static_cast<OutT *>(a.vis_out);
+    const double *uvw = a.uvw;
+    const double *wn = a.wavenumbers;
     const int nvis = it.nt * g.nch;
     for (int b = 0; b < nvis; b += kDegridThreads * kDegridVpt) {
         float du[kDegridVpt], dv[kDegridVpt], dw[kDegridVpt], ar[kDegridVpt], ai[kDegridVpt];
@@ -139,8 +148,8 @@ __global__ void __launch_bounds__(kDegridThreads) degridder_fp32_kernel(const Gr
             if (j < nvis) {
                 const int t = it.t0 + j / g.nch, ch = j - (j / g.nch) * g.nch;
                 const int64_t row = static_cast<int64_t>(sg.bl) * g.nt_all + t;
-                const double *q = a.uvw + row * 3;
-                const double kw = a.wavenumbers[ch];
+                const double *q = uvw + row * 3;
+                const double kw = wn[ch];
                 du[k] = static_cast<float>(uoff - kw * q[0]);
                 dv[k] = static_cast<float>(voff - kw * q[1]);
                 dw[k] = static_cast<float>(woff - kw * q[2]);
@@ -171,63 +180,75 @@ __global__ void __launch_bounds__(kDegridThreads) degridder_fp32_kernel(const Gr
         for (int k = 0; k < kDegridVpt; k++)
             if (idx[k] >= 0) store_vis(out, idx[k], make_float2(ar[k] * g.inv_s2, ai[k] * g.inv_s2));
     }
+    if (BATCH) {
+        __syncthreads();
+        if (tid == 0) note_item_done(a.done, a.finish_ns);
+    }
 }
 
-template <int S>
-cudaError_t gridder_dispatch_vis(const GridderArgs &a, cudaStream_t st) {
+template <int S, bool BATCH>
+cudaError_t gridder_dispatch(const GridderArgs &a, cudaStream_t st, const GridderArgs *probs) {
     constexpr int NT = S * S / ppt_for(S);
     if (a.nitems == 0) return cudaSuccess;
     if (a.vis_c128)
-        gridder_fp32_kernel<S, double2><<<a.nitems, NT, 0, st>>>(a);
+        gridder_fp32_kernel<S, double2, BATCH><<<a.nitems, NT, 0, st>>>(a, probs);
     else
-        gridder_fp32_kernel<S, float2><<<a.nitems, NT, 0, st>>>(a);
+        gridder_fp32_kernel<S, float2, BATCH><<<a.nitems, NT, 0, st>>>(a, probs);
     return cudaGetLastError();
 }
 
-template <int S>
-cudaError_t degridder_dispatch(const GridderArgs &a, cudaStream_t st) {
+template <int S, bool BATCH>
+cudaError_t degridder_dispatch(const GridderArgs &a, cudaStream_t st, const GridderArgs *probs) {
     if (a.nitems == 0) return cudaSuccess;
     const size_t smem = sizeof(float4) * S * S;
     if (a.out_c128) {
-        cudaError_t e = cudaFuncSetAttribute(degridder_fp32_kernel<S, double2>,
+        cudaError_t e = cudaFuncSetAttribute(degridder_fp32_kernel<S, double2, BATCH>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
         if (e != cudaSuccess) return e;
-        degridder_fp32_kernel<S, double2><<<a.nitems, kDegridThreads, smem, st>>>(a);
+        degridder_fp32_kernel<S, double2, BATCH><<<a.nitems, kDegridThreads, smem, st>>>(a, probs);
     } else {
-        cudaError_t e = cudaFuncSetAttribute(degridder_fp32_kernel<S, float2>,
+        cudaError_t e = cudaFuncSetAttribute(degridder_fp32_kernel<S, float2, BATCH>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
         if (e != cudaSuccess) return e;
-        degridder_fp32_kernel<S, float2><<<a.nitems, kDegridThreads, smem, st>>>(a);
+        degridder_fp32_kernel<S, float2, BATCH><<<a.nitems, kDegridThreads, smem, st>>>(a, probs);
     }
     return cudaGetLastError();
+}
+
+template <bool BATCH>
+cudaError_t gridder_by_size(const GridderArgs &a, cudaStream_t st, const GridderArgs *probs) {
+    switch (a.g.S) {
+        case 8: return gridder_dispatch<8, BATCH>(a, st, probs);
+        case 16: return gridder_dispatch<16, BATCH>(a, st, probs);
+        case 24: return gridder_dispatch<24, BATCH>(a, st, probs);
+        case 32: return gridder_dispatch<32, BATCH>(a, st, probs);
+        case 48: return gridder_dispatch<48, BATCH>(a, st, probs);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+template <bool BATCH>
+cudaError_t degridder_by_size(const GridderArgs &a, cudaStream_t st, const GridderArgs *probs) {
+    switch (a.g.S) {
+        case 8: return degridder_dispatch<8, BATCH>(a, st, probs);
+        case 16: return degridder_dispatch<16, BATCH>(a, st, probs);
+        case 24: return degridder_dispatch<24, BATCH>(a, st, probs);
+        case 32: return degridder_dispatch<32, BATCH>(a, st, probs);
+        case 48: return degridder_dispatch<48, BATCH>(a, st, probs);
+        default: return cudaErrorInvalidValue;
+    }
 }
 
 }  // namespace
 
-bool fp32_subgrid_size_supported(int S) {
-    return S == 8 || S == 16 || S == 24 || S == 32 || S == 48;
+bool fp32_subgrid_size_supported(int S) { return S == 8 || S == 16 || S == 24 || S == 32 || S == 48; }
+
+cudaError_t launch_gridder_fp32(const GridderArgs &a, cudaStream_t st, const GridderArgs *probs) {
+    return probs ? gridder_by_size<true>(a, st, probs) : gridder_by_size<false>(a, st, nullptr);
 }
 
-cudaError_t launch_gridder_fp32(const GridderArgs &a, cudaStream_t st) {
-    switch (a.g.S) {
-        case 8: return gridder_dispatch_vis<8>(a, st);
-        case 16: return gridder_dispatch_vis<16>(a, st);
-        case 24: return gridder_dispatch_vis<24>(a, st);
-        case 32: return gridder_dispatch_vis<32>(a, st);
-        case 48: return gridder_dispatch_vis<48>(a, st);
-        default: return cudaErrorInvalidValue;
-    }
-}
-
-cudaError_t launch_degridder_fp32(const GridderArgs &a, cudaStream_t st) {
-    switch (a.g.S) {
-        case 8: return degridder_dispatch<8>(a, st);
-        case 16: return degridder_dispatch<16>(a, st);
-        case 24: return degridder_dispatch<24>(a, st);
-        case 32: return degridder_dispatch<32>(a, st);
-        case 48: return degridder_dispatch<48>(a, st);
-        default: return cudaErrorInvalidValue;
-    }
+cudaError_t launch_degridder_fp32(const GridderArgs &a, cudaStream_t st, const GridderArgs *probs) {
+    return probs ? degridder_by_size<true>(a, st, probs) : degridder_by_size<false>(a, st, nullptr);
 }
 
 }  // namespace p9idg

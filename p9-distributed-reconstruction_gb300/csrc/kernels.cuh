@@ -50,11 +50,31 @@ struct GridderArgs {
     bool out_c128;
     int32_t nsub;              // subgrids in `subs`
     int32_t *status;           // device status word
+    // batched launches: work items left in this problem; the CTA finishing the last one
+    // records the GPU time (ns) in *finish_ns.  Null when not tracked.
+    int32_t *done;
+    unsigned long long *finish_ns;
 };
 
-cudaError_t launch_gridder_fp32(const GridderArgs &a, cudaStream_t st);
-cudaError_t launch_degridder_fp32(const GridderArgs &a, cudaStream_t st);
+// Batched launches pass `probs` (device array of per-problem arguments, indexed by
+// WorkItem::problem); `a` then only supplies the launch-wide item list and sizes.
+cudaError_t launch_gridder_fp32(const GridderArgs &a, cudaStream_t st, const GridderArgs *probs = nullptr);
+cudaError_t launch_degridder_fp32(const GridderArgs &a, cudaStream_t st, const GridderArgs *probs = nullptr);
 bool fp32_subgrid_size_supported(int S);
+
+__device__ inline unsigned long long device_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Called by thread 0 after the block's last global store for an item: counts the item down
+// and stamps the problem's completion time when it was the last one.
+__device__ inline void note_item_done(int32_t *done, unsigned long long *finish_ns) {
+    if (!done) return;
+    __threadfence();
+    if (atomicSub(done, 1) == 1) *finish_ns = device_ns();
+}
 
 // ---- launchers (subgrid_ops.cu) ----
 struct SubgridOpArgs {
@@ -70,9 +90,10 @@ struct SubgridOpArgs {
     float2 *subgrids;          // split output [nsub][S][S]
     bool wstack;               // AdderWStack (mirror/conjugate negative w) vs Adder
     int32_t *status;
+    const int2 *refs;          // batched launches: (problem, subgrid) per block; nsub = count
 };
-cudaError_t launch_subgrid_ifft_add(const SubgridOpArgs &a, cudaStream_t st);
-cudaError_t launch_split_subgrid_fft(const SubgridOpArgs &a, cudaStream_t st);
+cudaError_t launch_subgrid_ifft_add(const SubgridOpArgs &a, cudaStream_t st, const SubgridOpArgs *probs = nullptr);
+cudaError_t launch_split_subgrid_fft(const SubgridOpArgs &a, cudaStream_t st, const SubgridOpArgs *probs = nullptr);
 
 // ---- launchers (grid_ops.cu) ----
 // c128 (unshifted, host layout) -> c64 shifted copy and, when out128 != null, c128 shifted copy.

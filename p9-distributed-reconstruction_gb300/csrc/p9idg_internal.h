@@ -20,12 +20,14 @@ struct DevSubgrid {
     int32_t item_count;      // number of gridder work items
 };
 
-// A (subgrid, time chunk) unit of gridder or degridder work (16 bytes).
+// A (subgrid, time chunk) unit of gridder or degridder work (24 bytes).
 struct WorkItem {
     int32_t subgrid;
     int32_t t0;      // first time sample of the chunk
     int32_t nt;      // time samples in the chunk
     int32_t slot;    // gridder: index of this item's partial subgrid buffer
+    int32_t problem; // batched launches: index of the imaging problem (plan) it belongs to
+    int32_t pad;
 };
 
 // Scalars every kernel needs.

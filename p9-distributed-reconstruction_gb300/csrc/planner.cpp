@@ -244,7 +244,7 @@ void build_work_items(const std::vector<p9idg_subgrid> &subs, int32_t nch, int64
         d = {s.baseline_idx, s.time_sample_start, s.time_sample_count, s.u_pixel, s.v_pixel, s.w_lambda, slot, 0};
         for (int32_t t = 0; t < s.time_sample_count; t += chunk) {
             const int32_t len = std::min(chunk, s.time_sample_count - t);
-            items.push_back({static_cast<int32_t>(i), s.time_sample_start + t, len, slot++});
+            items.push_back({static_cast<int32_t>(i), s.time_sample_start + t, len, slot++, 0, 0});
             d.item_count++;
         }
     }

@@ -70,14 +70,30 @@ __device__ void load_twiddles(float2 *tw, int sign) {
     }
 }
 
-template <int S, bool WSTACK>
-__global__ void __launch_bounds__(kThreads) subgrid_ifft_add_kernel(const SubgridOpArgs a) {
+// Block -> (arguments, subgrid index): its own launch, or the (problem, subgrid) pair of a batch.
+template <bool BATCH>
+__device__ __forceinline__ const SubgridOpArgs &block_args(const SubgridOpArgs &L, const SubgridOpArgs *probs,
+                                                          int &sidx) {
+    if (BATCH) {
+        const int2 r = L.refs[blockIdx.x];
+        sidx = r.y;
+        return probs[r.x];
+    }
+    sidx = blockIdx.x;
+    return L;
+}
+
+template <int S, bool WSTACK, bool BATCH>
+__global__ void __launch_bounds__(kThreads)
+    subgrid_ifft_add_kernel(const SubgridOpArgs L, const SubgridOpArgs *__restrict__ probs) {
     __shared__ float2 buf[S][S + 1];
     __shared__ float2 tmp[S][S + 1];
     __shared__ float2 tw[S];
-    const Geometry &g = a.g;
+    int sidx;
+    const SubgridOpArgs &a = block_args<BATCH>(L, probs, sidx);
+    const Geometry g = a.g;
     const int N = g.N;
-    const DevSubgrid sg = a.subs[blockIdx.x];
+    const DevSubgrid sg = a.subs[sidx];
     int sx = sg.u, sy = sg.v, sw = sg.w;
     bool neg = false;
     if (WSTACK) {
@@ -131,14 +147,17 @@ __global__ void __launch_bounds__(kThreads) subgrid_ifft_add_kernel(const Subgri
     }
 }
 
-template <int S, bool WSTACK>
-__global__ void __launch_bounds__(kThreads) split_subgrid_fft_kernel(const SubgridOpArgs a) {
+template <int S, bool WSTACK, bool BATCH>
+__global__ void __launch_bounds__(kThreads)
+    split_subgrid_fft_kernel(const SubgridOpArgs L, const SubgridOpArgs *__restrict__ probs) {
     __shared__ float2 buf[S][S + 1];
     __shared__ float2 tmp[S][S + 1];
     __shared__ float2 tw[S];
-    const Geometry &g = a.g;
+    int sidx;
+    const SubgridOpArgs &a = block_args<BATCH>(L, probs, sidx);
+    const Geometry g = a.g;
     const int N = g.N;
-    const DevSubgrid sg = a.subs[blockIdx.x];
+    const DevSubgrid sg = a.subs[sidx];
     const int sx = sg.u, sy = sg.v;
     const bool neg = WSTACK && sg.w < 0;
     const bool in_range = WSTACK ? (sx >= 1 && sx < N - S && sy >= 1 && sy < N - S)
@@ -164,52 +183,62 @@ __global__ void __launch_bounds__(kThreads) split_subgrid_fft_kernel(const Subgr
     }
     __syncthreads();
     dft_2d<S>(buf, tmp, tw, 1.0f);
-    float2 *out = a.subgrids + static_cast<int64_t>(blockIdx.x) * S * S;
+    float2 *out = a.subgrids + static_cast<int64_t>(sidx) * S * S;
     for (int i = threadIdx.x; i < S * S; i += kThreads) out[i] = buf[i / S][i % S];
 }
 
-template <int S>
-cudaError_t ifft_add_dispatch(const SubgridOpArgs &a, cudaStream_t st) {
+template <int S, bool BATCH>
+cudaError_t ifft_add_dispatch(const SubgridOpArgs &a, cudaStream_t st, const SubgridOpArgs *probs) {
     if (a.nsub == 0) return cudaSuccess;
     if (a.wstack)
-        subgrid_ifft_add_kernel<S, true><<<a.nsub, kThreads, 0, st>>>(a);
+        subgrid_ifft_add_kernel<S, true, BATCH><<<a.nsub, kThreads, 0, st>>>(a, probs);
     else
-        subgrid_ifft_add_kernel<S, false><<<a.nsub, kThreads, 0, st>>>(a);
+        subgrid_ifft_add_kernel<S, false, BATCH><<<a.nsub, kThreads, 0, st>>>(a, probs);
     return cudaGetLastError();
 }
 
-template <int S>
-cudaError_t split_dispatch(const SubgridOpArgs &a, cudaStream_t st) {
+template <int S, bool BATCH>
+cudaError_t split_dispatch(const SubgridOpArgs &a, cudaStream_t st, const SubgridOpArgs *probs) {
     if (a.nsub == 0) return cudaSuccess;
     if (a.wstack)
-        split_subgrid_fft_kernel<S, true><<<a.nsub, kThreads, 0, st>>>(a);
+        split_subgrid_fft_kernel<S, true, BATCH><<<a.nsub, kThreads, 0, st>>>(a, probs);
     else
-        split_subgrid_fft_kernel<S, false><<<a.nsub, kThreads, 0, st>>>(a);
+        split_subgrid_fft_kernel<S, false, BATCH><<<a.nsub, kThreads, 0, st>>>(a, probs);
     return cudaGetLastError();
+}
+
+template <bool BATCH>
+cudaError_t ifft_add_by_size(const SubgridOpArgs &a, cudaStream_t st, const SubgridOpArgs *probs) {
+    switch (a.g.S) {
+        case 8: return ifft_add_dispatch<8, BATCH>(a, st, probs);
+        case 16: return ifft_add_dispatch<16, BATCH>(a, st, probs);
+        case 24: return ifft_add_dispatch<24, BATCH>(a, st, probs);
+        case 32: return ifft_add_dispatch<32, BATCH>(a, st, probs);
+        case 48: return ifft_add_dispatch<48, BATCH>(a, st, probs);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+template <bool BATCH>
+cudaError_t split_by_size(const SubgridOpArgs &a, cudaStream_t st, const SubgridOpArgs *probs) {
+    switch (a.g.S) {
+        case 8: return split_dispatch<8, BATCH>(a, st, probs);
+        case 16: return split_dispatch<16, BATCH>(a, st, probs);
+        case 24: return split_dispatch<24, BATCH>(a, st, probs);
+        case 32: return split_dispatch<32, BATCH>(a, st, probs);
+        case 48: return split_dispatch<48, BATCH>(a, st, probs);
+        default: return cudaErrorInvalidValue;
+    }
 }
 
 }  // namespace
 
-cudaError_t launch_subgrid_ifft_add(const SubgridOpArgs &a, cudaStream_t st) {
-    switch (a.g.S) {
-        case 8: return ifft_add_dispatch<8>(a, st);
-        case 16: return ifft_add_dispatch<16>(a, st);
-        case 24: return ifft_add_dispatch<24>(a, st);
-        case 32: return ifft_add_dispatch<32>(a, st);
-        case 48: return ifft_add_dispatch<48>(a, st);
-        default: return cudaErrorInvalidValue;
-    }
+cudaError_t launch_subgrid_ifft_add(const SubgridOpArgs &a, cudaStream_t st, const SubgridOpArgs *probs) {
+    return probs ? ifft_add_by_size<true>(a, st, probs) : ifft_add_by_size<false>(a, st, nullptr);
 }
 
-cudaError_t launch_split_subgrid_fft(const SubgridOpArgs &a, cudaStream_t st) {
-    switch (a.g.S) {
-        case 8: return split_dispatch<8>(a, st);
-        case 16: return split_dispatch<16>(a, st);
-        case 24: return split_dispatch<24>(a, st);
-        case 32: return split_dispatch<32>(a, st);
-        case 48: return split_dispatch<48>(a, st);
-        default: return cudaErrorInvalidValue;
-    }
+cudaError_t launch_split_subgrid_fft(const SubgridOpArgs &a, cudaStream_t st, const SubgridOpArgs *probs) {
+    return probs ? split_by_size<true>(a, st, probs) : split_by_size<false>(a, st, nullptr);
 }
 
 }  // namespace p9idg

@@ -101,23 +101,6 @@ __device__ __forceinline__ uint32_t chunk_off(int row, int kg) {
     return static_cast<uint32_t>((row >> 3) * 1024 + kg * 128 + (row & 7) * 16);
 }
 
-struct TcArgs {
-    Geometry g;
-    const WorkItem *items;
-    const DevSubgrid *subs;
-    const int64_t *coef_off;
-    const float4 *coef;
-    const void *vis;
-    const float *lmn;   // l[S], n[S*S]
-    const float *tabs;  // f[S], r[S*S]
-    const float *taper;
-    float2 *partials;
-    const float2 *subgrids;
-    void *vis_out;
-    int32_t *status;
-    float dw_scale;  // FP16 operands: power of two bringing max |dw| below 1 (1 for BF16)
-    float r_scale;   // FP16 operands: power of two bringing max |r| below 1 (1 for BF16)
-};
 
 // 2^-e with m * 2^-e in [0.5, 1) (1 for m == 0): exact power-of-two scale
 __device__ __forceinline__ float pow2_scale(float m) {
@@ -181,8 +164,8 @@ constexpr uint32_t kGStageBytes = kGStageA + kGStageB;
 constexpr uint32_t kGSmem = kGStages * kGStageBytes + kGRing * kGRingSlot + 512 + 1024;
 constexpr uint32_t kGTmemCols = 64;
 
-template <bool BF16, typename VisT>
-__global__ void __launch_bounds__(kGThreads, 2) tc_gridder_kernel(const TcArgs a) {
+template <bool BF16, typename VisT, bool BATCH>
+__global__ void __launch_bounds__(kGThreads, 2) tc_gridder_kernel(const TcArgs L, const TcArgs *__restrict__ probs) {
     extern __shared__ unsigned char smem_raw[];
     unsigned char *smem = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     unsigned char *ring = smem + kGStages * kGStageBytes;
@@ -196,8 +179,9 @@ __global__ void __launch_bounds__(kGThreads, 2) tc_gridder_kernel(const TcArgs a
     float *red = reinterpret_cast<float *>(tmem_slot + 2);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const Geometry &g = a.g;
-    const WorkItem it = a.items[blockIdx.x];
+    const WorkItem it = L.items[blockIdx.x];
+    const TcArgs &a = BATCH ? probs[it.problem] : L;
+    const Geometry g = a.g;
     const DevSubgrid sg = a.subs[it.subgrid];
     const int nvis = it.nt * g.nch;
     const int nstages = (nvis + kGVps - 1) / kGVps;
@@ -424,8 +408,8 @@ constexpr uint32_t kDTileBytes = 2 * kDTileHalf;
 constexpr uint32_t kDSmem = kDStatic + 2 * kDTileBytes + kDRing * kDRingSlot + 256 + 512 + 1024;
 constexpr uint32_t kDTmemCols = 256;
 
-template <bool BF16, typename OutT>
-__global__ void __launch_bounds__(kDThreads, 2) tc_degridder_kernel(const TcArgs a) {
+template <bool BF16, typename OutT, bool BATCH>
+__global__ void __launch_bounds__(kDThreads, 2) tc_degridder_kernel(const TcArgs L, const TcArgs *__restrict__ probs) {
     extern __shared__ unsigned char smem_raw[];
     unsigned char *smem = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     unsigned char *bstat = smem;
@@ -444,8 +428,9 @@ __global__ void __launch_bounds__(kDThreads, 2) tc_degridder_kernel(const TcArgs
     float *red = reinterpret_cast<float *>(tmem_slot + 2);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const Geometry &g = a.g;
-    const WorkItem it = a.items[blockIdx.x];
+    const WorkItem it = L.items[blockIdx.x];
+    const TcArgs &a = BATCH ? probs[it.problem] : L;
+    const Geometry g = a.g;
     const DevSubgrid sg = a.subs[it.subgrid];
     const int nvis = it.nt * g.nch;
     const int ntiles = (nvis + kDTile - 1) / kDTile;
@@ -701,6 +686,7 @@ __global__ void __launch_bounds__(kDThreads, 2) tc_degridder_kernel(const TcArgs
         tc_fence_after();
         tmem_dealloc(tmem, kDTmemCols);
     }
+    if (BATCH && threadIdx.x == 0) note_item_done(a.done, a.finish_ns);  // every visibility store is done
 }
 
 // ---------------- self-test GEMM: C[128][N] = A[128][64] . B[N][64]^T ----------------
@@ -840,7 +826,7 @@ p9idg_status tc_prepare(TcPlanState &st, const std::vector<p9idg_subgrid> &subs,
     // degridder work items: whole time samples, up to 4096 visibilities each
     std::vector<DevSubgrid> dtmp;
     std::vector<WorkItem> ditems;
-    build_work_items(subs, nch, 4096, dtmp, ditems);
+    build_work_items(subs, nch, st.degrid_chunk, dtmp, ditems);
     st.ncoef = off.back();
     cudaError_t e;
     if ((e = cudaMalloc(&st.coef, sizeof(float4) * std::max<int64_t>(1, st.ncoef))) != cudaSuccess ||
@@ -860,6 +846,7 @@ p9idg_status tc_prepare(TcPlanState &st, const std::vector<p9idg_subgrid> &subs,
         return P9IDG_CUDA_ERROR;
     }
     st.nditems = static_cast<int32_t>(ditems.size());
+    st.ditems_host = ditems;
     st.S = S;
     st.ready = true;
     return P9IDG_OK;
@@ -881,33 +868,24 @@ static p9idg_status launch_coef(TcPlanState &st, const GridderArgs &a, int32_t n
     return P9IDG_OK;
 }
 
-p9idg_status tc_grid(TcPlanState &st, const GridderArgs &a, int mode, cudaStream_t stream, std::string &err) {
-    if (!st.ready) {
-        err = "tensor-core state not prepared";
-        return P9IDG_INVALID_ARGUMENT;
-    }
-    p9idg_status s = launch_coef(st, a, a.nsub, stream, err);
-    if (s != P9IDG_OK || a.nitems == 0) return s;
-    TcArgs t{};
-    fill_args(t, a, st);
-    t.items = a.items;
-    t.vis = a.vis;
-    t.partials = a.partials;
-    t.status = a.status;
+template <bool BATCH>
+static p9idg_status launch_tc_gridder(const TcArgs &t, const TcArgs *probs, int32_t nitems, bool c128, int mode,
+                                      cudaStream_t stream, std::string &err) {
+    if (nitems == 0) return P9IDG_OK;
     const bool bf16 = mode == P9IDG_MODE_TC_BF16X3;
     cudaError_t e;
-    if (bf16 && a.vis_c128) {
-        e = set_smem(tc_gridder_kernel<true, double2>, kGSmem);
-        if (e == cudaSuccess) tc_gridder_kernel<true, double2><<<a.nitems, kGThreads, kGSmem, stream>>>(t);
+    if (bf16 && c128) {
+        e = set_smem(tc_gridder_kernel<true, double2, BATCH>, kGSmem);
+        if (e == cudaSuccess) tc_gridder_kernel<true, double2, BATCH><<<nitems, kGThreads, kGSmem, stream>>>(t, probs);
     } else if (bf16) {
-        e = set_smem(tc_gridder_kernel<true, float2>, kGSmem);
-        if (e == cudaSuccess) tc_gridder_kernel<true, float2><<<a.nitems, kGThreads, kGSmem, stream>>>(t);
-    } else if (a.vis_c128) {
-        e = set_smem(tc_gridder_kernel<false, double2>, kGSmem);
-        if (e == cudaSuccess) tc_gridder_kernel<false, double2><<<a.nitems, kGThreads, kGSmem, stream>>>(t);
+        e = set_smem(tc_gridder_kernel<true, float2, BATCH>, kGSmem);
+        if (e == cudaSuccess) tc_gridder_kernel<true, float2, BATCH><<<nitems, kGThreads, kGSmem, stream>>>(t, probs);
+    } else if (c128) {
+        e = set_smem(tc_gridder_kernel<false, double2, BATCH>, kGSmem);
+        if (e == cudaSuccess) tc_gridder_kernel<false, double2, BATCH><<<nitems, kGThreads, kGSmem, stream>>>(t, probs);
     } else {
-        e = set_smem(tc_gridder_kernel<false, float2>, kGSmem);
-        if (e == cudaSuccess) tc_gridder_kernel<false, float2><<<a.nitems, kGThreads, kGSmem, stream>>>(t);
+        e = set_smem(tc_gridder_kernel<false, float2, BATCH>, kGSmem);
+        if (e == cudaSuccess) tc_gridder_kernel<false, float2, BATCH><<<nitems, kGThreads, kGSmem, stream>>>(t, probs);
     }
     if (e == cudaSuccess) e = cudaGetLastError();
     if (e != cudaSuccess) {
@@ -917,33 +895,24 @@ p9idg_status tc_grid(TcPlanState &st, const GridderArgs &a, int mode, cudaStream
     return P9IDG_OK;
 }
 
-p9idg_status tc_degrid(TcPlanState &st, const GridderArgs &a, int mode, cudaStream_t stream, std::string &err) {
-    if (!st.ready) {
-        err = "tensor-core state not prepared";
-        return P9IDG_INVALID_ARGUMENT;
-    }
-    p9idg_status s = launch_coef(st, a, a.nsub, stream, err);
-    if (s != P9IDG_OK || st.nditems == 0) return s;
-    TcArgs t{};
-    fill_args(t, a, st);
-    t.items = static_cast<const WorkItem *>(st.ditems);
-    t.subgrids = a.subgrids;
-    t.vis_out = a.vis_out;
-    t.status = a.status;
+template <bool BATCH>
+static p9idg_status launch_tc_degridder(const TcArgs &t, const TcArgs *probs, int32_t nitems, bool c128, int mode,
+                                        cudaStream_t stream, std::string &err) {
+    if (nitems == 0) return P9IDG_OK;
     const bool bf16 = mode == P9IDG_MODE_TC_BF16X3;
     cudaError_t e;
-    if (bf16 && a.out_c128) {
-        e = set_smem(tc_degridder_kernel<true, double2>, kDSmem);
-        if (e == cudaSuccess) tc_degridder_kernel<true, double2><<<st.nditems, kDThreads, kDSmem, stream>>>(t);
+    if (bf16 && c128) {
+        e = set_smem(tc_degridder_kernel<true, double2, BATCH>, kDSmem);
+        if (e == cudaSuccess) tc_degridder_kernel<true, double2, BATCH><<<nitems, kDThreads, kDSmem, stream>>>(t, probs);
     } else if (bf16) {
-        e = set_smem(tc_degridder_kernel<true, float2>, kDSmem);
-        if (e == cudaSuccess) tc_degridder_kernel<true, float2><<<st.nditems, kDThreads, kDSmem, stream>>>(t);
-    } else if (a.out_c128) {
-        e = set_smem(tc_degridder_kernel<false, double2>, kDSmem);
-        if (e == cudaSuccess) tc_degridder_kernel<false, double2><<<st.nditems, kDThreads, kDSmem, stream>>>(t);
+        e = set_smem(tc_degridder_kernel<true, float2, BATCH>, kDSmem);
+        if (e == cudaSuccess) tc_degridder_kernel<true, float2, BATCH><<<nitems, kDThreads, kDSmem, stream>>>(t, probs);
+    } else if (c128) {
+        e = set_smem(tc_degridder_kernel<false, double2, BATCH>, kDSmem);
+        if (e == cudaSuccess) tc_degridder_kernel<false, double2, BATCH><<<nitems, kDThreads, kDSmem, stream>>>(t, probs);
     } else {
-        e = set_smem(tc_degridder_kernel<false, float2>, kDSmem);
-        if (e == cudaSuccess) tc_degridder_kernel<false, float2><<<st.nditems, kDThreads, kDSmem, stream>>>(t);
+        e = set_smem(tc_degridder_kernel<false, float2, BATCH>, kDSmem);
+        if (e == cudaSuccess) tc_degridder_kernel<false, float2, BATCH><<<nitems, kDThreads, kDSmem, stream>>>(t, probs);
     }
     if (e == cudaSuccess) e = cudaGetLastError();
     if (e != cudaSuccess) {
@@ -951,6 +920,57 @@ p9idg_status tc_degrid(TcPlanState &st, const GridderArgs &a, int mode, cudaStre
         return P9IDG_CUDA_ERROR;
     }
     return P9IDG_OK;
+}
+
+void tc_fill_args(const TcPlanState &st, const GridderArgs &a, TcArgs &t) {
+    fill_args(t, a, st);
+    t.items = a.items;
+    t.vis = a.vis;
+    t.partials = a.partials;
+    t.subgrids = a.subgrids;
+    t.vis_out = a.vis_out;
+    t.status = a.status;
+    t.done = a.done;
+    t.finish_ns = a.finish_ns;
+}
+
+p9idg_status tc_coefs(TcPlanState &st, const GridderArgs &a, cudaStream_t stream, std::string &err) {
+    if (!st.ready) {
+        err = "tensor-core state not prepared";
+        return P9IDG_INVALID_ARGUMENT;
+    }
+    return launch_coef(st, a, a.nsub, stream, err);
+}
+
+p9idg_status tc_grid(TcPlanState &st, const GridderArgs &a, int mode, cudaStream_t stream, std::string &err) {
+    p9idg_status s = tc_coefs(st, a, stream, err);
+    if (s != P9IDG_OK) return s;
+    TcArgs t{};
+    tc_fill_args(st, a, t);
+    return launch_tc_gridder<false>(t, nullptr, a.nitems, a.vis_c128, mode, stream, err);
+}
+
+p9idg_status tc_degrid(TcPlanState &st, const GridderArgs &a, int mode, cudaStream_t stream, std::string &err) {
+    p9idg_status s = tc_coefs(st, a, stream, err);
+    if (s != P9IDG_OK) return s;
+    TcArgs t{};
+    tc_fill_args(st, a, t);
+    t.items = static_cast<const WorkItem *>(st.ditems);
+    return launch_tc_degridder<false>(t, nullptr, st.nditems, a.out_c128, mode, stream, err);
+}
+
+p9idg_status tc_grid_batch(const TcArgs *probs, const WorkItem *items, int32_t nitems, int mode,
+                           cudaStream_t stream, std::string &err) {
+    TcArgs t{};
+    t.items = items;
+    return launch_tc_gridder<true>(t, probs, nitems, false, mode, stream, err);
+}
+
+p9idg_status tc_degrid_batch(const TcArgs *probs, const WorkItem *items, int32_t nitems, int mode,
+                             cudaStream_t stream, std::string &err) {
+    TcArgs t{};
+    t.items = items;
+    return launch_tc_degridder<true>(t, probs, nitems, false, mode, stream, err);
 }
 
 void tc_release(TcPlanState &st) {

@@ -19,12 +19,45 @@ struct TcPlanState {
     void *tables = nullptr;       // float: f[S] (separable part of n), r[S*S] (remainder)
     void *ditems = nullptr;       // degridder work items (<= 2048 visibilities)
     int32_t nditems = 0;
+    std::vector<WorkItem> ditems_host;  // the same list on the host (batches merge them)
+    int64_t degrid_chunk = 4096;        // visibilities per degridder work item (set before tc_prepare)
     double max_w_r = 0;           // max |dw| * max |r|: size of the neglected second-order term
     float dw_scale = 1.f;         // FP16 mode: power of two with max |dw| * dw_scale < 1
     float r_scale = 1.f;          // FP16 mode: power of two with max |r| * r_scale < 1
 };
 
+// Arguments of one problem for the tensor-core kernels.
+struct TcArgs {
+    Geometry g;
+    const WorkItem *items;
+    const DevSubgrid *subs;
+    const int64_t *coef_off;
+    const float4 *coef;
+    const void *vis;
+    const float *lmn;   // l[S], n[S*S]
+    const float *tabs;  // f[S], r[S*S]
+    const float *taper;
+    float2 *partials;
+    const float2 *subgrids;
+    void *vis_out;
+    int32_t *status;
+    float dw_scale;  // FP16 operands: power of two bringing max |dw| below 1 (1 for BF16)
+    float r_scale;   // FP16 operands: power of two bringing max |r| below 1 (1 for BF16)
+    int32_t *done;   // batched launches: completion count / time (see GridderArgs)
+    unsigned long long *finish_ns;
+};
+
 bool tc_subgrid_size_supported(int S);
+// Per-problem arguments of a prepared plan (host side; device pointers inside).
+void tc_fill_args(const TcPlanState &st, const GridderArgs &a, TcArgs &t);
+// Coefficients for the plan's current uvw (no-op when still valid).
+p9idg_status tc_coefs(TcPlanState &st, const GridderArgs &a, cudaStream_t stream, std::string &err);
+// One launch over the work items of many problems; `probs` is a device array of TcArgs
+// indexed by WorkItem::problem.
+p9idg_status tc_grid_batch(const TcArgs *probs, const WorkItem *items, int32_t nitems, int mode,
+                           cudaStream_t stream, std::string &err);
+p9idg_status tc_degrid_batch(const TcArgs *probs, const WorkItem *items, int32_t nitems, int mode,
+                             cudaStream_t stream, std::string &err);
 // Builds the tables and uploads them (once per plan).
 p9idg_status tc_prepare(TcPlanState &st, const std::vector<p9idg_subgrid> &subs, const std::vector<float> &lmn,
                         int S, int nch, const std::vector<double> &wn, const double *uvw_host, int nt_all,

@@ -383,6 +383,80 @@ class FFT:
         return out
 
 
+class Tuning(ctypes.Structure):
+    _fields_ = [("subgrid_size", ctypes.c_int32), ("kernel_size", ctypes.c_int32),
+                ("gridder_max_vis", ctypes.c_int32), ("degridder_max_vis", ctypes.c_int32),
+                ("seconds_per_gridded_vis", ctypes.c_double), ("gridded_fraction", ctypes.c_double)]
+
+
+def autotune(c: GriddingConstants, uvw, frequencies, mode=nat.MODE_FP32, subgrid_sizes=None) -> dict:
+    """p9idg_autotune: subgrid size and work-item sizes timed on a sample of the baselines."""
+    uvw = _f64(uvw)
+    freq = _f64(frequencies)
+    sizes = None if subgrid_sizes is None else np.ascontiguousarray(subgrid_sizes, np.int32)
+    out = Tuning()
+    pr = c.native()
+    _check(nat.lib().p9idg_autotune(ctypes.byref(pr), _ptr(uvw), uvw.shape[0], uvw.shape[1], _ptr(freq), len(freq),
+                                    int(mode), _ptr(sizes), 0 if sizes is None else len(sizes), ctypes.byref(out)))
+    return {k: getattr(out, k) for k, _ in Tuning._fields_}
+
+
+class Batch:
+    """p9idg_batch: many plans gridded/degridded with one launch per kernel stage.
+
+    Device buffers (raw pointers, complex64) are fixed at creation: per plan its
+    visibilities, w layers (output of grid_w), model grid (input of degrid_w) and
+    degridded visibilities."""
+
+    def __init__(self, plans, d_vis, d_layers, d_grids, d_vis_out):
+        n = len(plans)
+        arr = lambda xs: (ctypes.c_void_p * n)(*[ctypes.c_void_p(int(x)) for x in xs])  # noqa: E731
+        self._plans = list(plans)  # keep the plans alive
+        self._h = ctypes.c_void_p()
+        _check(nat.lib().p9idg_batch_create((ctypes.c_void_p * n)(*[p.handle for p in plans]), n, arr(d_vis),
+                                            arr(d_layers), arr(d_grids), arr(d_vis_out), ctypes.byref(self._h)))
+
+    def grid_w(self):
+        _check(nat.lib().p9idg_batch_grid_w(self._h))
+
+    def degrid_w(self):
+        _check(nat.lib().p9idg_batch_degrid_w(self._h))
+
+    def capture_graph(self):
+        _check(nat.lib().p9idg_batch_capture_graph(self._h))
+
+    def run(self):
+        _check(nat.lib().p9idg_batch_run(self._h))
+
+    def synchronize(self):
+        _check(nat.lib().p9idg_batch_synchronize(self._h))
+
+    def latencies_ms(self) -> np.ndarray:
+        out = np.zeros(len(self._plans), np.float64)
+        _check(nat.lib().p9idg_batch_latencies(self._h, _ptr(out)))
+        return out
+
+    def stream(self) -> int:
+        s = ctypes.c_void_p()
+        _check(nat.lib().p9idg_batch_get_stream(self._h, ctypes.byref(s)))
+        return s.value or 0
+
+    def destroy(self):
+        if getattr(self, "_h", None) and self._h.value:
+            nat.lib().p9idg_batch_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+
+def set_chunking(plan: Plan, gridder_max_vis: int, degridder_max_vis: int):
+    _check(nat.lib().p9idg_plan_set_chunking(plan.handle, int(gridder_max_vis), int(degridder_max_vis)))
+
+
 def device_count() -> int:
     return int(nat.lib().p9idg_device_count())
 

@@ -227,6 +227,41 @@ WORKLOADS = {
 }
 
 
+def batched_workloads(n=64, seed=4, subgrid_size=32, w_layers=8):
+    """Independent imaging problems of mixed sizes: images 512^2..2048^2, 200-2000 times,
+    4-32 channels, 16-64 antennas (log-radial within 8 km), 1.5 arcsec cells, the sky of
+    the 3072^2 workload (power-law points + Gaussians)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        N = 2 * int(rng.integers(256, 1025))
+        obs = dict(seed=seed * 1000 + i, n_ant=int(rng.integers(16, 65)), array_diameter_m=8000.0,
+                   layout="log_radial", nt=int(rng.integers(200, 2001)), dump_s=10.0, f_lo=1.2e9, f_hi=1.5e9,
+                   nch=int(rng.integers(4, 33)), grid_size=N, cell_arcsec=1.5, n_power_law=2000, n_gauss=20,
+                   noise_sigma=1e-3)
+        out.append(dict(obs=obs, grid=dict(subgrid_size=subgrid_size, kernel_size=8, max_timesteps=1024,
+                                           w_layers=w_layers)))
+    return out
+
+
+def build_geometry(workload):
+    """uvw, frequencies and gridding constants of a workload without its sky (cheap)."""
+    o, g = workload["obs"], workload["grid"]
+    rng = np.random.default_rng(o["seed"])
+    if o["layout"] == "uniform":
+        ants = antennas_uniform_disk(rng, o["n_ant"], o["array_diameter_m"])
+    else:
+        ants = antennas_log_radial(rng, o["n_ant"], o["array_diameter_m"])
+    uvw = earth_rotation_uvw(ants, o.get("lat_deg", -30.7215), o.get("dec_deg", -70.0), o["nt"], o["dump_s"])
+    freqs = np.linspace(o["f_lo"], o["f_hi"], o["nch"])
+    cell = cell_rad(o["cell_arcsec"])
+    consts = dict(vis_count=int(uvw.shape[0] * uvw.shape[1] * o["nch"]), grid_size=o["grid_size"],
+                  subgrid_size=g["subgrid_size"], kernel_size=g["kernel_size"], max_timesteps=g["max_timesteps"],
+                  scale_arcsec=float(np.float32(cell)), wlayer_count=g["w_layers"],
+                  wstep=wstep_for(uvw, freqs, g["w_layers"]))
+    return uvw, freqs, consts
+
+
 def scaled_workload(name, *, n_ant=None, nt=None, nch=None, seed=None):
     """A copy of a workload with fewer antennas/times/channels (parity-test sizes)."""
     w = WORKLOADS[name]
