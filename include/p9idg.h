@@ -118,6 +118,11 @@ p9idg_status p9idg_plan_set_taper(p9idg_plan *plan, const float *taper);
 /* Runs the plan's work on a caller's cudaStream_t (NULL = the plan's own stream). */
 p9idg_status p9idg_plan_set_stream(p9idg_plan *plan, void *cuda_stream);
 p9idg_status p9idg_plan_get_stream(const p9idg_plan *plan, void **cuda_stream);
+/* The GriddingConstants the plan was made with. */
+p9idg_status p9idg_plan_get_params(const p9idg_plan *plan, p9idg_params *out);
+/* Creates the plan's device state (stream, constant tables) on the current device now; the
+ * device entry points otherwise do this on first use. */
+p9idg_status p9idg_plan_init_device(p9idg_plan *plan);
 void p9idg_plan_destroy(p9idg_plan *plan);
 
 /* ---------------- IDG facade, host arrays (Core/ImageDomainGridder/IDG.cs) ---------------- */
@@ -225,6 +230,102 @@ typedef struct p9idg_tuning {
 p9idg_status p9idg_autotune(const p9idg_params *c, const double *uvw, int32_t nbl, int32_t nt,
                             const double *frequencies, int32_t nch, int32_t mode, const int32_t *subgrid_sizes,
                             int32_t nsizes, p9idg_tuning *out);
+
+/* ---------------- deconvolution side of the serial major cycle ---------------- */
+
+/* FastSerialCD (Core/Deconvolution/FastSerialCD.cs), the IDeconvolver of the serial major cycle,
+ * on the GPU with the reference's float arithmetic: the same pixel sequence, values and
+ * iteration count.  Created like `new FastSerialCD(totalSize, psf)` (FastSerialCD.cs:31-46):
+ * total size n x n, square PSF; PSF^2 (PSF.CalcPSFSquared) and the Lipschitz map
+ * (PSF.CalcAMap) are built on the device. */
+typedef struct p9idg_cd p9idg_cd;
+/* DeconvolutionResult (IDeconvolver.cs:9-21). */
+typedef struct p9idg_cd_result {
+    int32_t converged;
+    int32_t iterations;
+    double elapsed_ms;
+} p9idg_cd_result;
+p9idg_status p9idg_cd_create(int32_t n, const float *psf, int32_t psf_h, int32_t psf_w, p9idg_cd **out);
+/* FastSerialCD.MaxLipschitz (max of PSF^2). */
+p9idg_status p9idg_cd_max_lipschitz(const p9idg_cd *cd, float *out);
+/* Copies of the device PSF^2 ([2 psf_h][2 psf_w]) and Lipschitz map ([n][n]); either may be NULL. */
+p9idg_status p9idg_cd_get_maps(p9idg_cd *cd, float *psf2_out, float *amap_out);
+p9idg_status p9idg_cd_psf2_size(const p9idg_cd *cd, int32_t *h, int32_t *w);
+/* Stream for the calls below (NULL = the deconvolver's own). */
+p9idg_status p9idg_cd_set_stream(p9idg_cd *cd, void *cuda_stream);
+/* FastSerialCD.Deconvolve (FastSerialCD.cs:76-102, 111-114): x (reconstruction) and bmap
+ * (gradients) float[n][n] are updated in place, as the reference does.  P9IDG_INVALID_ARGUMENT
+ * where the reference would index pixel (-1, -1) (epsilon <= 0 and no pixel changes). */
+p9idg_status p9idg_cd_deconvolve(p9idg_cd *cd, float *x, float *bmap, float lambda, float alpha, int32_t max_iter,
+                                 float epsilon, p9idg_cd_result *result);
+p9idg_status p9idg_cd_deconvolve_device(p9idg_cd *cd, float *d_x, float *d_bmap, float lambda, float alpha,
+                                        int32_t max_iter, float epsilon, p9idg_cd_result *result);
+/* FastSerialCD.DeconvolvePath (FastSerialCD.cs:49-74, 106-109). */
+p9idg_status p9idg_cd_deconvolve_path(p9idg_cd *cd, float *x, float *bmap, float lambda_min, float lambda_factor,
+                                      float alpha, int32_t max_path_iter, int32_t max_iter, float epsilon,
+                                      p9idg_cd_result *result);
+/* FastSerialCD.GetAbsMaxDiff (FastSerialCD.cs:129-132). */
+p9idg_status p9idg_cd_get_abs_max_diff(p9idg_cd *cd, const float *x, const float *bmap, float lambda, float alpha,
+                                       float *out);
+p9idg_status p9idg_cd_get_abs_max_diff_device(p9idg_cd *cd, const float *d_x, const float *d_bmap, float lambda,
+                                              float alpha, float *out);
+/* FastSerialCD.ResetLipschitzMap (FastSerialCD.cs:116-127), square PSF. */
+p9idg_status p9idg_cd_reset_lipschitz_map(p9idg_cd *cd, const float *psf, int32_t h, int32_t w);
+void p9idg_cd_destroy(p9idg_cd *cd);
+
+/* PaddedConvolver (Core/PaddedConvolver.cs) in FP64 on the device.  _create takes the Fourier
+ * kernel as `new PaddedConvolver(Complex[,] kernel, Rectangle kernelSize)` does (:36-41);
+ * _create_correlation builds it from a PSF on the device, = new PaddedConvolver(
+ * PSF.CalcPaddedFourierCorrelation(psf, (0, 0, n, n)), psf rectangle) (MajorCycle.cs:73). */
+typedef struct p9idg_convolver p9idg_convolver;
+p9idg_status p9idg_convolver_create(const double *kernel, int32_t h, int32_t w, int32_t kernel_h, int32_t kernel_w,
+                                    p9idg_convolver **out);
+p9idg_status p9idg_convolver_create_correlation(const float *psf, int32_t psf_h, int32_t psf_w, int32_t n,
+                                                p9idg_convolver **out);
+/* PaddedConvolver.Convolve (PaddedConvolver.cs:43-65): image float[n][n] -> out float[n][n]. */
+p9idg_status p9idg_convolver_convolve(p9idg_convolver *conv, const float *image, int32_t n, float *out);
+p9idg_status p9idg_convolver_convolve_device(p9idg_convolver *conv, const float *d_image, int32_t n, float *d_out);
+void p9idg_convolver_destroy(p9idg_convolver *conv);
+
+/* PSF helpers (Core/Common.cs) computed on the device.
+ * CalcPaddedFourierCorrelation (:123-139): out complex[pad_y + h][pad_x + w] (must be square).
+ * CalcPSFSquared (:162-174): out float[2h][2w].  CalcAMap(psf, (0, 0, total_h, total_w)) (:76-105). */
+p9idg_status p9idg_psf_padded_fourier_correlation(const float *psf, int32_t h, int32_t w, int32_t pad_y,
+                                                  int32_t pad_x, double *out);
+p9idg_status p9idg_psf_squared(const float *psf, int32_t h, int32_t w, float *out);
+p9idg_status p9idg_psf_amap(const float *psf, int32_t h, int32_t w, int32_t total_h, int32_t total_w, float *out);
+
+/* MajorCycle.ReconstructSerialCD (SingleReconstruction/MajorCycle.cs:33-134) with the plan's
+ * gridder (its precision mode), FastSerialCD and the padded correlation, all on the device;
+ * the FITS writes of the reference are left out. */
+typedef struct p9idg_mc_params {
+    int32_t psf_cut_factor;     /* psfCutFactor */
+    int32_t max_major_cycles;   /* maxMajorCycle */
+    int32_t deconv_iterations;  /* deconvIterations */
+    int32_t reserved;
+    float lambda, alpha;
+    float deconv_epsilon;       /* deconvEpsilon */
+    float major_epsilon;        /* MAJOR_EPSILON, 1e-4f in the reference (MajorCycle.cs:18) */
+} p9idg_mc_params;
+/* What one major cycle computed, and its device time per phase. */
+typedef struct p9idg_mc_cycle {
+    float max_dirty, max_b, current_lambda, abs_max;
+    int32_t deconvolved, converged, iterations, reserved;
+    double grid_ms;    /* IDG.GridW of the residual visibilities */
+    double image_ms;   /* WStackIFFTFloat + Shift + the gradient correlation */
+    double deconv_ms;  /* GetAbsMaxDiff + Deconvolve */
+    double degrid_ms;  /* model FFT + IDG.DeGridW + Visibilities.Substract */
+} p9idg_mc_cycle;
+/* Host arrays: vis complex128[nbl][nt][nch] (data.Visibilities), flags 1 byte per sample;
+ * model_out (xImage) and residual_out (the last cycle's dirty image) float[N][N]; psf_out may be
+ * NULL; cycles[max_major_cycles]; *ncycles = cycles run. */
+p9idg_status p9idg_major_cycle_serial_cd(p9idg_plan *plan, const p9idg_mc_params *params, const double *vis,
+                                         const uint8_t *flags, float *model_out, float *residual_out, float *psf_out,
+                                         p9idg_mc_cycle *cycles, int32_t *ncycles);
+/* Device buffers: d_vis complex64, d_flags uint8, d_model / d_residual / d_psf (may be NULL) float[N][N]. */
+p9idg_status p9idg_major_cycle_serial_cd_device(p9idg_plan *plan, const p9idg_mc_params *params, const void *d_vis,
+                                                const uint8_t *d_flags, float *d_model, float *d_residual,
+                                                float *d_psf, p9idg_mc_cycle *cycles, int32_t *ncycles);
 
 /* ---------------- stage timing (CUDA events on the plan's stream) ---------------- */
 

@@ -75,6 +75,30 @@ def lib():
         L.oc_vis_subtract.argtypes = [P, P, P, i64, P]
         L.oc_num_threads.restype = ctypes.c_int
         L.oc_set_num_threads.argtypes = [ctypes.c_int]
+        f32, f64 = ctypes.c_float, ctypes.c_double
+        L.ocd_elastic_net_penalty.argtypes = [P, i32, i32, f32, f32]
+        L.ocd_elastic_net_penalty.restype = f64
+        L.ocd_get_max.argtypes = [P, i64]
+        L.ocd_get_max.restype = f32
+        L.ocd_residual_penalty.argtypes = [P, i64]
+        L.ocd_residual_penalty.restype = f64
+        L.ocd_max_lipschitz.argtypes = [P, i32, i32]
+        L.ocd_max_lipschitz.restype = f64
+        L.ocd_psf_cut.argtypes = [P, i32, i32, P]
+        L.ocd_max_sidelobe.argtypes = [P, i32, i32]
+        L.ocd_max_sidelobe.restype = f32
+        L.ocd_amap_scan.argtypes = [P, i32, i32, P]
+        L.ocd_amap.argtypes = [P, i32, i32, i32, i32, i32, i32, i32, i32, P]
+        L.ocd_padded_fourier_correlation.argtypes = [P, i32, i32, i32, i32, P]
+        L.ocd_padded_convolve.argtypes = [P, i32, i32, i32, i32, P, i32, P]
+        L.ocd_psf_squared.argtypes = [P, i32, i32, P]
+        L.ocd_get_abs_max_diff.argtypes = [P, P, P, i32, f32, f32]
+        L.ocd_get_abs_max_diff.restype = f32
+        L.ocd_get_abs_max_pixel.argtypes = [P, P, P, i32, f32, f32, P, P]
+        L.ocd_get_abs_max_pixel.restype = f32
+        L.ocd_deconvolve.argtypes = [P, P, P, i32, P, i32, i32, f32, f32, i32, f32, P, P]
+        L.ocd_major_cycle.argtypes = [P, P, i64, P, i32, i32, P, i32, P, P, i32, i32, f32, f32, i32, f32,
+                                      P, P, P, P, P]
         _lib = L
     return _lib
 
@@ -304,3 +328,136 @@ def num_threads():
 
 def set_num_threads(n):
     lib().oc_set_num_threads(int(n))
+
+
+# ---------- deconvolution side of the serial major cycle (deconv_oracle.c) ----------
+
+INDEX_OUT_OF_RANGE = 10
+
+CYCLE_DTYPE = np.dtype([("max_dirty", "<f4"), ("max_b", "<f4"), ("current_lambda", "<f4"), ("abs_max", "<f4"),
+                        ("deconvolved", "<i4"), ("converged", "<i4"), ("iterations", "<i4"), ("pad", "<i4")])
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, np.float32)
+
+
+def elastic_net_penalty(img, lam, alpha):
+    img = _f32(img)
+    return lib().ocd_elastic_net_penalty(_p(img), img.shape[0], img.shape[1], float(lam), float(alpha))
+
+
+def get_max(img):
+    img = _f32(img)
+    return float(lib().ocd_get_max(_p(img), img.size))
+
+
+def residual_penalty(img):
+    img = _f32(img)
+    return lib().ocd_residual_penalty(_p(img), img.size)
+
+
+def max_lipschitz(psf):
+    psf = _f32(psf)
+    return lib().ocd_max_lipschitz(_p(psf), psf.shape[0], psf.shape[1])
+
+
+def psf_cut(psf, factor):
+    psf = _f32(psf)
+    m = psf.shape[0] // factor
+    out = np.zeros((m, m), np.float32)
+    lib().ocd_psf_cut(_p(psf), psf.shape[0], int(factor), _p(out))
+    return out
+
+
+def max_sidelobe(psf, factor):
+    psf = _f32(psf)
+    return float(lib().ocd_max_sidelobe(_p(psf), psf.shape[0], int(factor)))
+
+
+def amap_scan(psf):
+    psf = _f32(psf)
+    out = np.zeros(psf.shape, np.float64)
+    lib().ocd_amap_scan(_p(psf), psf.shape[0], psf.shape[1], _p(out))
+    return out
+
+
+def amap(psf, total, section=None):
+    """PSF.CalcAMap(psf, totalSize=(0,0,*total), imageSection=(y, x, yEnd, xEnd))."""
+    psf = _f32(psf)
+    sy, sx, sye, sxe = section if section is not None else (0, 0, total[0], total[1])
+    out = np.zeros((sye - sy, sxe - sx), np.float32)
+    lib().ocd_amap(_p(psf), psf.shape[0], psf.shape[1], int(total[0]), int(total[1]), sy, sx, sye, sxe, _p(out))
+    return out
+
+
+def padded_fourier_correlation(psf, pad):
+    psf = _f32(psf)
+    out = np.zeros((pad[0] + psf.shape[0], pad[1] + psf.shape[1]), np.complex128)
+    _check(lib().ocd_padded_fourier_correlation(_p(psf), psf.shape[0], psf.shape[1], int(pad[0]), int(pad[1]),
+                                                _p(out)), "PSF.CalcPaddedFourierCorrelation")
+    return out
+
+
+def padded_convolve(kernel, kernel_rect, img):
+    kernel = _c128(kernel)
+    img = _f32(img)
+    out = np.zeros(img.shape, np.float32)
+    _check(lib().ocd_padded_convolve(_p(kernel), kernel.shape[0], kernel.shape[1], int(kernel_rect[0]),
+                                     int(kernel_rect[1]), _p(img), img.shape[0], _p(out)), "PaddedConvolver.Convolve")
+    return out
+
+
+def psf_squared(psf):
+    psf = _f32(psf)
+    out = np.zeros((2 * psf.shape[0], 2 * psf.shape[1]), np.float32)
+    _check(lib().ocd_psf_squared(_p(psf), psf.shape[0], psf.shape[1], _p(out)), "PSF.CalcPSFSquared")
+    return out
+
+
+def get_abs_max_diff(x, g, a, lam, alpha):
+    x, g, a = _f32(x), _f32(g), _f32(a)
+    return float(lib().ocd_get_abs_max_diff(_p(x), _p(g), _p(a), x.shape[0], float(lam), float(alpha)))
+
+
+def get_abs_max_pixel(x, g, a, lam, alpha):
+    """FastSerialCD.GetAbsMax -> (y, x, diff, new value)."""
+    x, g, a = _f32(x), _f32(g), _f32(a)
+    yx = np.zeros(2, np.int32)
+    xn = np.zeros(1, np.float32)
+    d = lib().ocd_get_abs_max_pixel(_p(x), _p(g), _p(a), x.shape[0], float(lam), float(alpha), _p(yx), _p(xn))
+    return int(yx[0]), int(yx[1]), float(d), float(xn[0])
+
+
+def deconvolve(x, g, a, psf2, lam, alpha, iterations, epsilon):
+    """FastSerialCD.Deconvolve on copies -> (x, g, converged, iterations)."""
+    x, g = _f32(x).copy(), _f32(g).copy()
+    a, psf2 = _f32(a), _f32(psf2)
+    conv = np.zeros(1, np.int32)
+    it = np.zeros(1, np.int32)
+    _check(lib().ocd_deconvolve(_p(x), _p(g), _p(a), x.shape[0], _p(psf2), psf2.shape[0], psf2.shape[1], float(lam),
+                                float(alpha), int(iterations), float(epsilon), _p(conv), _p(it)),
+           "FastSerialCD.Deconvolve")
+    return x, g, bool(conv[0]), int(it[0])
+
+
+def major_cycle(consts, subs, uvw, freq, vis, flags, psf_cut_factor, max_major, lam, alpha, deconv_iterations,
+                deconv_epsilon):
+    """MajorCycle.ReconstructSerialCD with FastSerialCD -> dict(model, residual, psf, cycles)."""
+    N = consts["grid_size"]
+    subs = np.ascontiguousarray(subs, SUBGRID_DTYPE)
+    uvw, freq = np.ascontiguousarray(uvw, np.float64), np.ascontiguousarray(freq, np.float64)
+    vis = _c128(vis)
+    flags = np.ascontiguousarray(flags, np.uint8)
+    nbl, nt = uvw.shape[0], uvw.shape[1]
+    model = np.zeros((N, N), np.float32)
+    resid = np.zeros((N, N), np.float32)
+    psf = np.zeros((N, N), np.float32)
+    cycles = np.zeros(max(1, max_major), CYCLE_DTYPE)
+    nc = np.zeros(1, np.int32)
+    pr = params(consts)
+    _check(lib().ocd_major_cycle(ctypes.byref(pr), _p(subs), len(subs), _p(uvw), nbl, nt, _p(freq), len(freq),
+                                 _p(vis), _p(flags), int(psf_cut_factor), int(max_major), float(lam), float(alpha),
+                                 int(deconv_iterations), float(deconv_epsilon), _p(model), _p(resid), _p(psf),
+                                 _p(cycles), _p(nc)), "MajorCycle.ReconstructSerialCD")
+    return dict(model=model, residual=resid, psf=psf, cycles=cycles[:nc[0]])

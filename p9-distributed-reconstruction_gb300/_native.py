@@ -53,7 +53,7 @@ class PlanInfo(ctypes.Structure):
 
 # name -> (restype, argtypes); every symbol include/p9idg.h declares
 P = ctypes.c_void_p
-i32, i64, dbl = ctypes.c_int32, ctypes.c_int64, ctypes.c_double
+i32, i64, dbl, f32 = ctypes.c_int32, ctypes.c_int64, ctypes.c_double, ctypes.c_float
 SIGNATURES = {
     "p9idg_plan_create": (i32, [P, P, i32, i32, P, i32, ctypes.POINTER(P)]),
     "p9idg_plan_create_from_subgrids": (i32, [P, P, i64, P, i32, i32, P, i32, ctypes.POINTER(P)]),
@@ -103,6 +103,30 @@ SIGNATURES = {
     "p9idg_batch_get_stream": (i32, [P, ctypes.POINTER(P)]),
     "p9idg_batch_destroy": (None, [P]),
     "p9idg_autotune": (i32, [P, P, i32, i32, P, i32, i32, P, i32, P]),
+    "p9idg_plan_get_params": (i32, [P, P]),
+    "p9idg_plan_init_device": (i32, [P]),
+    "p9idg_cd_create": (i32, [i32, P, i32, i32, ctypes.POINTER(P)]),
+    "p9idg_cd_max_lipschitz": (i32, [P, ctypes.POINTER(f32)]),
+    "p9idg_cd_get_maps": (i32, [P, P, P]),
+    "p9idg_cd_psf2_size": (i32, [P, ctypes.POINTER(i32), ctypes.POINTER(i32)]),
+    "p9idg_cd_set_stream": (i32, [P, P]),
+    "p9idg_cd_deconvolve": (i32, [P, P, P, f32, f32, i32, f32, P]),
+    "p9idg_cd_deconvolve_device": (i32, [P, P, P, f32, f32, i32, f32, P]),
+    "p9idg_cd_deconvolve_path": (i32, [P, P, P, f32, f32, f32, i32, i32, f32, P]),
+    "p9idg_cd_get_abs_max_diff": (i32, [P, P, P, f32, f32, ctypes.POINTER(f32)]),
+    "p9idg_cd_get_abs_max_diff_device": (i32, [P, P, P, f32, f32, ctypes.POINTER(f32)]),
+    "p9idg_cd_reset_lipschitz_map": (i32, [P, P, i32, i32]),
+    "p9idg_cd_destroy": (None, [P]),
+    "p9idg_convolver_create": (i32, [P, i32, i32, i32, i32, ctypes.POINTER(P)]),
+    "p9idg_convolver_create_correlation": (i32, [P, i32, i32, i32, ctypes.POINTER(P)]),
+    "p9idg_convolver_convolve": (i32, [P, P, i32, P]),
+    "p9idg_convolver_convolve_device": (i32, [P, P, i32, P]),
+    "p9idg_convolver_destroy": (None, [P]),
+    "p9idg_psf_padded_fourier_correlation": (i32, [P, i32, i32, i32, i32, P]),
+    "p9idg_psf_squared": (i32, [P, i32, i32, P]),
+    "p9idg_psf_amap": (i32, [P, i32, i32, i32, i32, P]),
+    "p9idg_major_cycle_serial_cd": (i32, [P, P, P, P, P, P, P, P, ctypes.POINTER(i32)]),
+    "p9idg_major_cycle_serial_cd_device": (i32, [P, P, P, P, P, P, P, P, ctypes.POINTER(i32)]),
 }
 
 _lib = None

@@ -784,6 +784,17 @@ p9idg_status p9idg_plan_get_stream(const p9idg_plan *plan, void **cuda_stream) {
     return P9IDG_OK;
 }
 
+p9idg_status p9idg_plan_get_params(const p9idg_plan *plan, p9idg_params *out) {
+    if (!plan || !out) return fail(P9IDG_INVALID_ARGUMENT, "null argument");
+    *out = plan->c;
+    return P9IDG_OK;
+}
+
+p9idg_status p9idg_plan_init_device(p9idg_plan *plan) {
+    if (!plan) return fail(P9IDG_INVALID_ARGUMENT, "null plan");
+    return ensure_device(plan);
+}
+
 void p9idg_plan_destroy(p9idg_plan *plan) {
     if (!plan) return;
     if (plan->dev_ready) {
