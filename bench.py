@@ -183,6 +183,92 @@ def run_reference(args):
     return 0
 
 
+def run_major_cycle(args):
+    """The full imaging loop on the 3072^2 workload: serial-CD major cycles (MajorCycle.cs:33-134,
+    lambda 1.0, alpha 0.01, PSF cut 8) with the BF16x3 gridder, beside the same loop with the
+    FP32 gridder; the FP64 CPU oracle runs the same loop on a small sample observation."""
+    import torch
+
+    pkg = entry.load_package()
+    synth = entry._load_module(entry.PKG_NAME + ".synth", os.path.join(entry.PKG_DIR, "synth.py"))
+    kw = dict(psfCutFactor=8, maxMajorCycle=args.mc_cycles, lambda_=1.0, alpha=0.01,
+              deconvIterations=args.mc_iterations, deconvEpsilon=1e-5)
+
+    def gpu_loop(obs, cd, mode_name, kwargs):
+        c = pkg.GriddingConstants.from_dict(cd)
+        N = cd["grid_size"]
+        part = pkg.Partitioner.CreatePartition(c, obs.uvw, obs.frequencies)
+        part.plan.set_mode(MODES[mode_name])
+        d_vis = torch.from_numpy(obs.vis.astype(np.complex64)).cuda()
+        d_flags = torch.from_numpy(obs.flags.astype(np.uint8)).cuda()
+        img = [torch.empty((N, N), dtype=torch.float32, device="cuda") for _ in range(3)]
+        ptrs = (part.plan, d_vis.data_ptr(), d_flags.data_ptr(), img[0].data_ptr(), img[1].data_ptr(),
+                img[2].data_ptr())
+        warm = dict(kwargs, maxMajorCycle=1, deconvIterations=min(10, kwargs["deconvIterations"]))
+        pkg.MajorCycle.reconstruct_serial_cd_device(*ptrs, **warm)  # module load, FFT plans
+        torch.cuda.synchronize()
+        clocks = ClockSampler(0)
+        clocks.start()
+        t0 = time.perf_counter()
+        cycles = pkg.MajorCycle.reconstruct_serial_cd_device(*ptrs, **kwargs)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        clk = clocks.stop()
+        return dict(wall_s=wall, cycles=cycles, model=img[0].cpu().numpy(), residual=img[1].cpu().numpy(),
+                    psf=img[2].cpu().numpy(), clocks=clk)
+
+    obs, cd = synth.build(WORKLOAD)
+    runs = {m: gpu_loop(obs, cd, m, kw) for m in ("tc_bf16x3", "fp32")}
+    tc, fp = runs["tc_bf16x3"], runs["fp32"]
+    iters = sum(int(c["iterations"]) for c in tc["cycles"])
+    deconv_s = sum(c["deconv_ms"] for c in tc["cycles"]) / 1e3
+
+    def rel(a, b):
+        return float(np.linalg.norm((a - b).ravel()) / max(np.linalg.norm(b.ravel()), 1e-30))
+
+    cpu = None
+    if not args.no_cpu_baseline:
+        oracle = load_oracle()
+        sobs, scd = synth.build(synth.scaled_workload("small_256", n_ant=16, nt=480, nch=8, seed=7))
+        subs = oracle.partition(scd, sobs.uvw, sobs.frequencies)
+        skw = dict(kw, maxMajorCycle=args.mc_cycles)
+        t0 = time.perf_counter()
+        ref = oracle.major_cycle(scd, subs, sobs.uvw, sobs.frequencies, sobs.vis, sobs.flags.astype(np.uint8),
+                                 skw["psfCutFactor"], skw["maxMajorCycle"], skw["lambda_"], skw["alpha"],
+                                 skw["deconvIterations"], skw["deconvEpsilon"])
+        cpu_s = time.perf_counter() - t0
+        g = gpu_loop(sobs, scd, "fp32", skw)
+        gt = gpu_loop(sobs, scd, "tc_bf16x3", skw)
+        nvis = int(np.prod(sobs.vis.shape))
+        cpu = {"value": cpu_s, "unit": "s per reconstruction", "cores": oracle.num_threads(), "kind": "port",
+               "sample": (f"the same loop on a 256^2 observation (16 antennas, 480 times, 8 channels: {nvis} "
+                          f"visibilities, {len(ref['cycles'])} cycles, "
+                          f"{int(ref['cycles']['iterations'].sum())} CD iterations), FP64 gridder"),
+               "gpu_fp32_same_sample_s": g["wall_s"], "gpu_tc_same_sample_s": gt["wall_s"],
+               "model_rel_l2_gpu_fp32_vs_cpu": rel(g["model"], ref["model"]),
+               "residual_rel_l2_gpu_fp32_vs_cpu": rel(g["residual"], ref["residual"]),
+               "model_rel_l2_gpu_tc_vs_cpu": rel(gt["model"], ref["model"]),
+               "residual_rel_l2_gpu_tc_vs_cpu": rel(gt["residual"], ref["residual"])}
+    slim = [{k: (round(v, 4) if isinstance(v, float) else v) for k, v in c.items()} for c in tc["cycles"]]
+    out = {"metric": f"s per {args.mc_cycles}-cycle serial-CD reconstruction at 3072^2 (BF16x3 gridder)",
+           "value": tc["wall_s"], "unit": "s", "n_gpus": 1, "steps": 1, "warmup": 1,
+           "ms_per_step": 1e3 * tc["wall_s"], "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+           "dtype": "tc_bf16x3 gridder, f32 images / coordinate descent, f64 correlation",
+           "data": "synthetic (seeded 3072^2 observation and sky)",
+           "config": {"workload": "3072^2: 2016 bl x 2000 t x 16 ch, S=32, W=8; PSF cut 8; "
+                                  f"lambda 1.0, alpha 0.01, <= {args.mc_iterations} CD iterations per cycle, eps 1e-5",
+                      "cycles_run": len(tc["cycles"])},
+           "cycles": slim,
+           "cd_iterations": iters, "cd_iterations_per_s": iters / deconv_s if deconv_s > 0 else None,
+           "fp32_gridder_s": fp["wall_s"],
+           "model_rel_l2_tc_vs_fp32": rel(tc["model"], fp["model"]),
+           "residual_rel_l2_tc_vs_fp32": rel(tc["residual"], fp["residual"]),
+           "psf_rel_l2_tc_vs_fp32": rel(tc["psf"], fp["psf"]),
+           "cpu_baseline": cpu, "clocks": tc["clocks"]}
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 def run_batched(args):
     """N independent problems (512^2..2048^2, 200-2000 times, 4-32 channels, 16-64 antennas):
     autotuned on the largest, gridded + degridded as one batch replayed from a CUDA graph."""
@@ -327,11 +413,17 @@ def main():
                     help="smaller array (fewer baselines) of the same workload, for profiling captures")
     ap.add_argument("--batched", type=int, default=0,
                     help="instead: N independent problems of mixed sizes in one batch (graph-replayed)")
+    ap.add_argument("--major-cycle", action="store_true",
+                    help="instead: the serial-CD major-cycle loop on the same workload")
+    ap.add_argument("--mc-cycles", type=int, default=6)
+    ap.add_argument("--mc-iterations", type=int, default=30000)
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
     if args.batched:
         return run_batched(args)
+    if args.major_cycle:
+        return run_major_cycle(args)
 
     import torch
 

@@ -12,12 +12,12 @@
 // changes it most (a scan of the whole image), sets it, and adds the scaled PSF^2 to the
 // gradient map in a window around it.  Only pixels in that window change, so the GPU keeps
 // the best candidate of every 32x128 tile and, per iteration, re-evaluates only the tiles the
-// window touches: one launch updates the window's gradients and those tiles' candidates, and
-// the launch's last CTA (an arrival counter, no waiting) reduces all tile candidates to the next
-// pixel.  A candidate is one 64-bit key, (|change| bits << 32) | (0xFFFFFFFF - pixel index),
+// window touches: one launch reduces the tile candidates the previous launch left to the
+// selected pixel (every CTA does this itself), updates the window's gradients and writes those
+// tiles' new candidates into the other of two state buffers.  A candidate is one 64-bit key, (|change| bits << 32) | (0xFFFFFFFF - pixel index),
 // so the largest key is the largest change and, among equal changes, the first pixel, which is
 // the order in which GetAbsMax (FastSerialCD.cs:135-170) keeps its winner.  Iterations are
-// launched from a captured CUDA graph, 128 at a time; a launch after the stopping iteration
+// launched from a captured CUDA graph, 256 at a time; a launch after the stopping iteration
 // does nothing, so the iteration count and result equal the reference's loop.
 
 #include <cuda_runtime.h>
@@ -112,24 +112,22 @@ __device__ __forceinline__ float prox(float x, float lipschitz, float lambda, fl
     return __fdiv_rn(num, den);
 }
 
-constexpr int kTY = 32, kTX = 128, kNT = 256, kWarps = kNT / 32;
-constexpr int kGraphIters = 128;
+constexpr int kTY = 32, kTX = 128, kNT = 512, kWarps = kNT / 32;
+constexpr int kGraphIters = 256;  // even: every replay ends on state buffer 0
+
+struct CdCtl {  // the state one launch hands to the next
+    int32_t iter, done, converged, error;
+};
 
 struct CdParams {  // device-resident, read by every launch (so one captured graph serves all calls)
     float *x, *g;
     const float *a, *psf2;
-    unsigned long long *tile_key;
-    float2 *tile_val;  // (new value, current value) of each tile's best pixel
+    unsigned long long *tile_key;  // [2][ntiles]: best key of each tile (double-buffered by launch parity)
+    float2 *tile_val;              // [2][ntiles]: (new value, current value) of each tile's best pixel
+    CdCtl *ctl;                    // [2]
     int32_t n, ph, pw, tiles_x, tiles_y, max_iter;
     float lambda, alpha, eps;
     int32_t pad;
-};
-
-struct CdCtl {
-    unsigned long long key;  // next pixel (0 = no pixel changes)
-    float xnew, xold;
-    int32_t iter, done, converged, error;
-    uint32_t arrive, pad;
 };
 
 __device__ __forceinline__ unsigned long long warp_max(unsigned long long v) {
@@ -140,62 +138,97 @@ __device__ __forceinline__ unsigned long long warp_max(unsigned long long v) {
     return v;
 }
 
+// Block-wide max with one barrier: every warp reduces the per-warp results itself.  sm[kWarps]
+// must not be reused by the same CTA afterwards (each call site has its own array).
 __device__ unsigned long long block_max(unsigned long long v, unsigned long long *sm) {
+    static_assert(kWarps <= 32, "one warp reduces the per-warp results");
     v = warp_max(v);
     if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = v;
     __syncthreads();
-    if (threadIdx.x < 32) {
-        v = threadIdx.x < kWarps ? sm[threadIdx.x] : 0ull;
-        v = warp_max(v);
-        if (threadIdx.x == 0) sm[kWarps] = v;
+    const unsigned lane = threadIdx.x & 31;
+    return warp_max(lane < kWarps ? sm[lane] : 0ull);
+}
+
+// The best key over all tiles of one buffer (8 loads in flight per thread: one round up to
+// 4096 tiles, e.g. a 4096^2 image).
+__device__ unsigned long long reduce_tiles(const unsigned long long *keys, int ntiles, unsigned long long *sm) {
+    unsigned long long best = 0;
+    for (int base = 0; base < ntiles; base += 8 * kNT) {
+        unsigned long long v[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            const int t = base + j * kNT + static_cast<int>(threadIdx.x);
+            v[j] = t < ntiles ? __ldcg(keys + t) : 0ull;
+        }
+#pragma unroll
+        for (int j = 0; j < 8; j++) best = v[j] > best ? v[j] : best;
     }
-    __syncthreads();
-    v = sm[kWarps];
-    __syncthreads();
-    return v;
+    return block_max(best, sm);
 }
 
 struct Window {
     uint32_t sel;  // selected pixel index
     int py, px, y0, y1, x0, x1, yh, xh;
-    float xnew, xdiff;
 };
 
-// Evaluates (and with UPDATE first updates) one tile; writes its best key and values.
+// Evaluates (and with UPDATE first updates) one tile; writes its best key and values.  All of a
+// thread's loads are issued before any is used (predicated, no early exits), so a tile costs one
+// memory latency rather than one per pixel.
 template <bool UPDATE>
 __device__ void eval_tile(const CdParams &P, float lambda, float alpha, int ty, int tx, const Window &w,
-                          unsigned long long *sm) {
+                          const float2 *s_val, unsigned long long *key_out, float2 *val_out, unsigned long long *sm) {
+    constexpr int R = kTY / kWarps, K = kTX / 32;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int yb = ty * kTY + warp * R, xb = tx * kTX + lane;
+    float gv[R][K], xv[R][K], av[R][K], pv[R][K];
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            const int y = yb + r, xc = xb + 32 * k;
+            const bool in = y < P.n && xc < P.n;
+            const uint32_t i = static_cast<uint32_t>(y) * static_cast<uint32_t>(P.n) + static_cast<uint32_t>(xc);
+            gv[r][k] = 0.0f;
+            xv[r][k] = 0.0f;
+            av[r][k] = 1.0f;
+            pv[r][k] = 0.0f;
+            if (in) {
+                gv[r][k] = P.g[i];
+                xv[r][k] = P.x[i];
+                av[r][k] = __ldg(P.a + i);
+            }
+            if (UPDATE && in && y >= w.y0 && y < w.y1 && xc >= w.x0 && xc < w.x1)
+                pv[r][k] = __ldg(P.psf2 + static_cast<int64_t>(y + w.yh - w.py) * P.pw + (xc + w.xh - w.px));
+        }
+    }
+    float xnew = 0.0f, xdiff = 0.0f;
+    if (UPDATE) {  // the selected pixel's values, loaded by thread 0 while the loads above were issued
+        __syncthreads();
+        xnew = s_val->x;
+        xdiff = __fsub_rn(s_val->y, s_val->x);  // pixelOld - maxPixel.PixelNew
+    }
     unsigned long long best = 0;
     float bnew = 0.0f, bold = 0.0f;
 #pragma unroll
-    for (int r = 0; r < kTY / kWarps; r++) {
-        const int y = ty * kTY + warp * (kTY / kWarps) + r;
-        if (y >= P.n) break;
+    for (int r = 0; r < R; r++) {
 #pragma unroll
-        for (int k = 0; k < kTX / 32; k++) {
-            const int xc = tx * kTX + lane + 32 * k;
-            if (xc >= P.n) break;
+        for (int k = 0; k < K; k++) {
+            const int y = yb + r, xc = xb + 32 * k;
+            if (y >= P.n || xc >= P.n) continue;
             const uint32_t i = static_cast<uint32_t>(y) * static_cast<uint32_t>(P.n) + static_cast<uint32_t>(xc);
-            float gv = P.g[i];
-            float old;
+            float g = gv[r][k], old = xv[r][k];
             if (UPDATE) {
                 if (y >= w.y0 && y < w.y1 && xc >= w.x0 && xc < w.x1) {
-                    const float p = P.psf2[static_cast<int64_t>(y + w.yh - w.py) * P.pw + (xc + w.xh - w.px)];
-                    gv = __fadd_rn(gv, __fmul_rn(p, w.xdiff));  // gradients[i, j] += psf2 * xDiff
-                    P.g[i] = gv;
+                    g = __fadd_rn(g, __fmul_rn(pv[r][k], xdiff));  // gradients[i, j] += psf2 * xDiff
+                    P.g[i] = g;
                 }
                 if (i == w.sel) {
-                    old = w.xnew;
-                    P.x[i] = w.xnew;
-                } else {
-                    old = P.x[i];
+                    old = xnew;
+                    P.x[i] = xnew;
                 }
-            } else {
-                old = P.x[i];
             }
-            const float av = P.a[i];
-            const float xt = prox(__fadd_rn(__fmul_rn(old, av), gv), av, lambda, alpha);
+            const float a = av[r][k];
+            const float xt = prox(__fadd_rn(__fmul_rn(old, a), g), a, lambda, alpha);
             const float d = fabsf(__fsub_rn(old, xt));
             const unsigned long long key =
                 (0.0f < d) ? ((static_cast<unsigned long long>(__float_as_uint(d)) << 32) | (0xFFFFFFFFu - i)) : 0ull;
@@ -208,112 +241,96 @@ __device__ void eval_tile(const CdParams &P, float lambda, float alpha, int ty, 
     }
     const unsigned long long m = block_max(best, sm);
     const int t = ty * P.tiles_x + tx;
-    if (threadIdx.x == 0) P.tile_key[t] = m;
-    if (m != 0ull && best == m) P.tile_val[t] = make_float2(bnew, bold);
+    if (threadIdx.x == 0) key_out[t] = m;
+    if (m != 0ull && best == m) val_out[t] = make_float2(bnew, bold);
 }
 
-// Every CTA of a launch arrives once; the last one reduces all tile candidates into ctl.
-__device__ void finish_launch(const CdParams &P, CdCtl *ctl, int32_t next_iter, bool init, unsigned long long *sm,
-                              int *s_last) {
-    __threadfence();
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        const uint32_t total = gridDim.x * gridDim.y;
-        *s_last = atomicAdd(&ctl->arrive, 1u) == total - 1u;
-    }
-    __syncthreads();
-    if (!*s_last) return;
-    __threadfence();
-    const int ntiles = P.tiles_x * P.tiles_y;
-    unsigned long long best = 0;
-    for (int t = threadIdx.x; t < ntiles; t += kNT) {
-        const unsigned long long k = __ldcg(P.tile_key + t);
-        best = k > best ? k : best;
-    }
-    best = block_max(best, sm);
-    if (threadIdx.x == 0) {
-        float xn = 0.0f, xo = 0.0f;
-        if (best) {
-            const uint32_t idx = 0xFFFFFFFFu - static_cast<uint32_t>(best);
-            const int t = static_cast<int>((idx / P.n) / kTY) * P.tiles_x + static_cast<int>((idx % P.n) / kTX);
-            const float2 v = __ldcg(P.tile_val + t);
-            xn = v.x;
-            xo = v.y;
-        }
-        ctl->key = best;
-        ctl->xnew = xn;
-        ctl->xold = xo;
-        ctl->iter = next_iter;
-        if (init) {
-            ctl->done = 0;
-            ctl->converged = 0;
-            ctl->error = 0;
-        }
-        __threadfence();
-        ctl->arrive = 0;
-    }
-}
-
-// Full scan: the candidate of every tile (GetAbsMax over the whole image).
-__global__ void __launch_bounds__(kNT) cd_scan_kernel(const CdParams *pp, float lambda, float alpha, CdCtl *ctl) {
-    __shared__ unsigned long long sm[kWarps + 1];
-    __shared__ int s_last;
+// Full scan into state buffer 0: the candidate of every tile (GetAbsMax over the whole image).
+__global__ void __launch_bounds__(kNT) cd_scan_kernel(const CdParams *pp, float lambda, float alpha) {
+    __shared__ unsigned long long sm[kWarps];
     const CdParams P = *pp;
     Window w{};
-    eval_tile<false>(P, lambda, alpha, blockIdx.y, blockIdx.x, w, sm);
-    finish_launch(P, ctl, 0, true, sm, &s_last);
+    eval_tile<false>(P, lambda, alpha, blockIdx.y, blockIdx.x, w, nullptr, P.tile_key, P.tile_val, sm);
+    if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) P.ctl[0] = CdCtl{0, 0, 0, 0};
 }
 
-// One coordinate-descent iteration (FastSerialCD.cs:83-98).
-__global__ void __launch_bounds__(kNT) cd_iter_kernel(const CdParams *pp, CdCtl *ctl) {
-    __shared__ unsigned long long sm[kWarps + 1];
-    __shared__ int s_last;
-    __shared__ CdCtl c;
-    if (threadIdx.x == 0) {
-        c.key = __ldcg(&ctl->key);
-        c.xnew = __ldcg(&ctl->xnew);
-        c.xold = __ldcg(&ctl->xold);
-        c.iter = __ldcg(&ctl->iter);
-        c.done = __ldcg(&ctl->done);
-    }
-    __syncthreads();
-    if (c.done) return;
+// The selected pixel's key and values of state buffer 0 (GetAbsMax's result), for the host.
+__global__ void __launch_bounds__(kNT) cd_pick_kernel(const CdParams *pp, unsigned long long *out_key, float2 *out_val) {
+    __shared__ unsigned long long sm[kWarps];
     const CdParams P = *pp;
+    const unsigned long long best = reduce_tiles(P.tile_key, P.tiles_x * P.tiles_y, sm);
+    if (threadIdx.x == 0) {
+        *out_key = best;
+        float2 v = make_float2(0.0f, 0.0f);
+        if (best) {
+            const uint32_t idx = 0xFFFFFFFFu - static_cast<uint32_t>(best);
+            v = P.tile_val[static_cast<int>((idx / P.n) / kTY) * P.tiles_x + static_cast<int>((idx % P.n) / kTX)];
+        }
+        *out_val = v;
+    }
+}
+
+// One coordinate-descent iteration (FastSerialCD.cs:83-98).  Launch k reads state buffer k % 2
+// (tile candidates and control) and writes buffer (k + 1) % 2: the window's tiles re-evaluated,
+// every other tile's candidate copied.  Each CTA finds the selected pixel itself from the input
+// buffer, so a launch needs no grid-wide synchronisation.
+__global__ void __launch_bounds__(kNT, 2) cd_iter_kernel(const CdParams *pp, int parity) {
+    __shared__ unsigned long long sm_in[kWarps], sm_out[kWarps];
+    __shared__ CdCtl c;
+    __shared__ float2 s_val;
+    const CdParams P = *pp;
+    const int ntiles = P.tiles_x * P.tiles_y;
+    const unsigned long long *kin = P.tile_key + static_cast<int64_t>(parity) * ntiles;
+    const float2 *vin = P.tile_val + static_cast<int64_t>(parity) * ntiles;
+    unsigned long long *kout = P.tile_key + static_cast<int64_t>(1 - parity) * ntiles;
+    float2 *vout = P.tile_val + static_cast<int64_t>(1 - parity) * ntiles;
+    const CdCtl *cin = P.ctl + parity;
+    CdCtl *cout = P.ctl + (1 - parity);
+    if (threadIdx.x == 0) c = *cin;
+    const unsigned long long key = reduce_tiles(kin, ntiles, sm_in);  // its barrier publishes c
     const bool lead = blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0;
+    if (c.done) {
+        if (lead) *cout = c;
+        return;
+    }
     if (c.iter >= P.max_iter) {  // while (!converged & iter < iterations)
-        if (lead) ctl->done = 1;
+        if (lead) *cout = CdCtl{c.iter, 1, 0, 0};
         return;
     }
-    const float diff = __uint_as_float(static_cast<uint32_t>(c.key >> 32));
+    const float diff = __uint_as_float(static_cast<uint32_t>(key >> 32));
     if (diff < P.eps) {  // converged = maxPixel.PixelMaxDiff < epsilon
-        if (lead) {
-            ctl->converged = 1;
-            ctl->done = 1;
-        }
+        if (lead) *cout = CdCtl{c.iter, 1, 1, 0};
         return;
     }
-    if (c.key == 0ull) {  // the reference would index pixel (-1, -1)
-        if (lead) {
-            ctl->error = 1;
-            ctl->done = 1;
-        }
+    if (key == 0ull) {  // the reference would index pixel (-1, -1)
+        if (lead) *cout = CdCtl{c.iter, 1, 0, 1};
         return;
     }
     Window w;
-    w.sel = 0xFFFFFFFFu - static_cast<uint32_t>(c.key);
+    w.sel = 0xFFFFFFFFu - static_cast<uint32_t>(key);
     w.py = static_cast<int>(w.sel / P.n);
     w.px = static_cast<int>(w.sel % P.n);
-    w.xnew = c.xnew;
-    w.xdiff = __fsub_rn(c.xold, c.xnew);  // pixelOld - maxPixel.PixelNew
     w.yh = P.ph / 2;
     w.xh = P.pw / 2;
     w.y0 = max(w.py - w.yh, 0);
     w.x0 = max(w.px - w.xh, 0);
     w.y1 = min(w.py - w.yh + P.ph, P.n);
     w.x1 = min(w.px - w.xh + P.pw, P.n);
-    const int ty = w.y0 / kTY + static_cast<int>(blockIdx.y), tx = w.x0 / kTX + static_cast<int>(blockIdx.x);
-    if (ty <= (w.y1 - 1) / kTY && tx <= (w.x1 - 1) / kTX) eval_tile<true>(P, P.lambda, P.alpha, ty, tx, w, sm);
-    finish_launch(P, ctl, c.iter + 1, false, sm, &s_last);
+    const int ty0 = w.y0 / kTY, ty1 = (w.y1 - 1) / kTY, tx0 = w.x0 / kTX, tx1 = (w.x1 - 1) / kTX;
+    // candidates of the tiles outside the window carry over unchanged
+    const int nb = gridDim.x * gridDim.y, b = blockIdx.y * gridDim.x + blockIdx.x;
+    for (int t = b + nb * static_cast<int>(threadIdx.x); t < ntiles; t += nb * kNT) {
+        const int tty = t / P.tiles_x, ttx = t % P.tiles_x;
+        if (tty < ty0 || tty > ty1 || ttx < tx0 || ttx > tx1) {
+            kout[t] = __ldcg(kin + t);
+            vout[t] = __ldcg(vin + t);
+        }
+    }
+    if (threadIdx.x == 0)
+        s_val = __ldcg(vin + static_cast<int>(w.py / kTY) * P.tiles_x + static_cast<int>(w.px / kTX));
+    const int ty = ty0 + static_cast<int>(blockIdx.y), tx = tx0 + static_cast<int>(blockIdx.x);
+    if (ty <= ty1 && tx <= tx1) eval_tile<true>(P, P.lambda, P.alpha, ty, tx, w, &s_val, kout, vout, sm_out);
+    if (lead) *cout = CdCtl{c.iter + 1, 0, 0, 0};
 }
 
 // ------------------------------------------------------------------------------------------
@@ -646,10 +663,11 @@ struct p9idg_cd {
     int n = 0, ph = 0, pw = 0;  // image size, psf2 size
     int tiles_x = 0, tiles_y = 0;
     float max_lipschitz = 0.0f;
-    Buf x, g, amap, psf2, tile_key, tile_val, params, ctl, word, partial, sq0, sq1, psf_tmp;
+    Buf x, g, amap, psf2, tile_key, tile_val, params, ctl, pick, word, partial, sq0, sq1, psf_tmp;
     Z2Z fft;
     CdParams hp{};
-    CdCtl *h_ctl = nullptr;  // pinned
+    CdCtl *h_ctl = nullptr;                // pinned
+    unsigned long long *h_pick = nullptr;  // pinned: selected key
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
 };
@@ -709,8 +727,7 @@ p9idg_status cd_capture(p9idg_cd *cd) {
     // captured on the deconvolver's own stream (never the legacy stream); replayed on cd->stream
     const dim3 grid = cd_window_grid(cd);
     CK(cudaStreamBeginCapture(cd->own, cudaStreamCaptureModeThreadLocal));
-    for (int k = 0; k < kGraphIters; k++)
-        cd_iter_kernel<<<grid, kNT, 0, cd->own>>>(cd->params.as<CdParams>(), cd->ctl.as<CdCtl>());
+    for (int k = 0; k < kGraphIters; k++) cd_iter_kernel<<<grid, kNT, 0, cd->own>>>(cd->params.as<CdParams>(), k & 1);
     cudaGraph_t gph = nullptr;
     CK(cudaStreamEndCapture(cd->own, &gph));
     cd->graph = gph;
@@ -718,11 +735,9 @@ p9idg_status cd_capture(p9idg_cd *cd) {
     return P9IDG_OK;
 }
 
-// GetAbsMax over the whole image with (lambda, alpha) into ctl: key, new and current value.
+// Candidates of every tile with (lambda, alpha) into state buffer 0, control reset.
 p9idg_status cd_scan(p9idg_cd *cd, float lambda, float alpha) {
-    CK(cudaMemsetAsync(cd->ctl.p, 0, sizeof(CdCtl), cd->stream));
-    cd_scan_kernel<<<dim3(cd->tiles_x, cd->tiles_y), kNT, 0, cd->stream>>>(cd->params.as<CdParams>(), lambda, alpha,
-                                                                           cd->ctl.as<CdCtl>());
+    cd_scan_kernel<<<dim3(cd->tiles_x, cd->tiles_y), kNT, 0, cd->stream>>>(cd->params.as<CdParams>(), lambda, alpha);
     CK(cudaGetLastError());
     return P9IDG_OK;
 }
@@ -769,8 +784,12 @@ p9idg_status cd_abs_max(p9idg_cd *cd, const float *d_x, const float *d_g, float 
     cd->hp.g = const_cast<float *>(d_g);
     TRY(cd_upload_params(cd));
     TRY(cd_scan(cd, lambda, alpha));
-    TRY(cd_read_ctl(cd));
-    const uint32_t bits = static_cast<uint32_t>(cd->h_ctl->key >> 32);
+    cd_pick_kernel<<<1, kNT, 0, cd->stream>>>(cd->params.as<CdParams>(), cd->pick.as<unsigned long long>(),
+                                             reinterpret_cast<float2 *>(cd->pick.as<unsigned long long>() + 1));
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(cd->h_pick, cd->pick.p, sizeof(unsigned long long), cudaMemcpyDeviceToHost, cd->stream));
+    CK(cudaStreamSynchronize(cd->stream));
+    const uint32_t bits = static_cast<uint32_t>(*cd->h_pick >> 32);
     std::memcpy(out, &bits, sizeof(float));
     return P9IDG_OK;
 }
@@ -780,10 +799,11 @@ void cd_release(p9idg_cd *cd) {
     if (cd->exec) cudaGraphExecDestroy(cd->exec);
     if (cd->graph) cudaGraphDestroy(cd->graph);
     Buf *bufs[] = {&cd->x, &cd->g, &cd->amap, &cd->psf2, &cd->tile_key, &cd->tile_val, &cd->params, &cd->ctl,
-                   &cd->word, &cd->partial, &cd->sq0, &cd->sq1, &cd->psf_tmp};
+                   &cd->pick, &cd->word, &cd->partial, &cd->sq0, &cd->sq1, &cd->psf_tmp};
     for (Buf *b : bufs) b->release();
     cd->fft.release();
     if (cd->h_ctl) cudaFreeHost(cd->h_ctl);
+    if (cd->h_pick) cudaFreeHost(cd->h_pick);
     if (cd->own) cudaStreamDestroy(cd->own);
 }
 
@@ -792,15 +812,17 @@ p9idg_status cd_init(p9idg_cd *cd, int n, const float *psf, int h, int w) {
     CK(cudaStreamCreateWithFlags(&cd->own, cudaStreamNonBlocking));
     cd->stream = cd->own;
     CK(cudaMallocHost(reinterpret_cast<void **>(&cd->h_ctl), sizeof(CdCtl)));
+    CK(cudaMallocHost(reinterpret_cast<void **>(&cd->h_pick), sizeof(unsigned long long)));
     cd->n = n;
     cd->tiles_x = (n + kTX - 1) / kTX;
     cd->tiles_y = (n + kTY - 1) / kTY;
     const size_t nn = static_cast<size_t>(n) * n, nt = static_cast<size_t>(cd->tiles_x) * cd->tiles_y;
     CK(cd->amap.ensure(sizeof(float) * nn));
-    CK(cd->tile_key.ensure(sizeof(unsigned long long) * nt));
-    CK(cd->tile_val.ensure(sizeof(float2) * nt));
+    CK(cd->tile_key.ensure(sizeof(unsigned long long) * 2 * nt));
+    CK(cd->tile_val.ensure(sizeof(float2) * 2 * nt));
     CK(cd->params.ensure(sizeof(CdParams)));
-    CK(cd->ctl.ensure(sizeof(CdCtl)));
+    CK(cd->ctl.ensure(sizeof(CdCtl) * 2));
+    CK(cd->pick.ensure(sizeof(unsigned long long) + sizeof(float2)));
     CK(cd->word.ensure(sizeof(unsigned int)));
     TRY(cd_set_maps(cd, psf, h, w));
     cd->hp = CdParams{};
@@ -808,6 +830,7 @@ p9idg_status cd_init(p9idg_cd *cd, int n, const float *psf, int h, int w) {
     cd->hp.psf2 = cd->psf2.as<float>();
     cd->hp.tile_key = cd->tile_key.as<unsigned long long>();
     cd->hp.tile_val = cd->tile_val.as<float2>();
+    cd->hp.ctl = cd->ctl.as<CdCtl>();
     cd->hp.n = n;
     cd->hp.ph = cd->ph;
     cd->hp.pw = cd->pw;
