@@ -532,10 +532,14 @@ def main():
         nvis = obs.vis.size
         h2d = nvis * 16 + 2 * obs.uvw.nbytes + N * N * 16
         d2h = W * N * N * 16 + N * N * 16 + nvis * 16
+        in_place = plan.host_access()
         e2e = {"value": ws * 2 * gridded * steps_e2e / t_e2e / 1e6, "unit": "Mvis/s",
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+               "host_arrays_in_place": in_place,
                "note": "IDG.GridW + IDG.DeGridW host API, Complex(double) arrays in pinned host memory, "
-                       "wall clock incl. H2D/D2H and complex128<->complex64 conversion"}
+                       "wall clock incl. every host<->device transfer and complex128<->complex64 conversion"
+                       + ("; the kernels read the visibilities and the model grid and write the degridded "
+                          "visibilities and the w layers in host memory over NVLink-C2C" if in_place else "")}
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:

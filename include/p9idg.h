@@ -123,6 +123,13 @@ p9idg_status p9idg_plan_get_params(const p9idg_plan *plan, p9idg_params *out);
 /* Creates the plan's device state (stream, constant tables) on the current device now; the
  * device entry points otherwise do this on first use. */
 p9idg_status p9idg_plan_init_device(p9idg_plan *plan);
+/* Host-array calls (p9idg_grid*, p9idg_degrid*): in_place = 1 (default) lets the kernels read the
+ * caller's visibilities and grid and write the degridded visibilities directly in host memory
+ * where the device reaches host memory through the host's page tables (NVLink-C2C on Grace),
+ * overlapping the link with the kernels; 0 stages every array through device copies.
+ * _get reports what the calls will do on this device (1 = in place). */
+p9idg_status p9idg_plan_set_host_access(p9idg_plan *plan, int32_t in_place);
+p9idg_status p9idg_plan_get_host_access(p9idg_plan *plan, int32_t *in_place);
 void p9idg_plan_destroy(p9idg_plan *plan);
 
 /* ---------------- IDG facade, host arrays (Core/ImageDomainGridder/IDG.cs) ---------------- */

@@ -105,6 +105,8 @@ SIGNATURES = {
     "p9idg_autotune": (i32, [P, P, i32, i32, P, i32, i32, P, i32, P]),
     "p9idg_plan_get_params": (i32, [P, P]),
     "p9idg_plan_init_device": (i32, [P]),
+    "p9idg_plan_set_host_access": (i32, [P, i32]),
+    "p9idg_plan_get_host_access": (i32, [P, ctypes.POINTER(i32)]),
     "p9idg_cd_create": (i32, [i32, P, i32, i32, ctypes.POINTER(P)]),
     "p9idg_cd_max_lipschitz": (i32, [P, ctypes.POINTER(f32)]),
     "p9idg_cd_get_maps": (i32, [P, P, P]),

@@ -136,6 +136,16 @@ struct p9idg_plan {
         d_flags, d_image;
     TcPlanState tc;
     FftCache fft;
+    // Host arrays used in place by the kernels (device reads/writes host memory through the host's
+    // page tables, e.g. NVLink-C2C on Grace systems) instead of staged through device copies.
+    bool host_direct = false;   // the device can access any host address
+    int32_t host_access = 1;    // caller's choice: 1 = in place where possible, 0 = staged copies
+    std::vector<int64_t> gaps;  // (start, count) ranges of visibilities no subgrid covers
+    std::vector<char> layer_used;  // w layers some subgrid adds into
+    bool gaps_ready = false;
+    DevBuf d_gaps;
+    cudaStream_t side = nullptr;  // the D2H copy of DeGrid's shifted grid runs here, beside the degridder
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 
     bool timing = false;
     std::vector<PendingTiming> pending;
@@ -263,6 +273,15 @@ p9idg_status ensure_device(p9idg_plan *p) {
     CK(cudaGetDevice(&p->device));
     CK(cudaStreamCreateWithFlags(&p->own_stream, cudaStreamNonBlocking));
     if (!p->stream) p->stream = p->own_stream;
+    CK(cudaStreamCreateWithFlags(&p->side, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&p->ev_fork, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&p->ev_join, cudaEventDisableTiming));
+    {
+        int pageable = 0, host_tables = 0;
+        CK(cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, p->device));
+        CK(cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, p->device));
+        p->host_direct = pageable != 0 && host_tables != 0;
+    }
     const int S = p->c.subgrid_size;
     CK(p->d_wn.ensure(sizeof(double) * std::max(1, p->nch)));
     CK(p->d_lmn.ensure(sizeof(float) * p->lmn.size()));
@@ -429,8 +448,12 @@ p9idg_status run_grid(p9idg_plan *p, const void *d_vis, bool vis_c128, float2 *d
 }
 
 // grid (device complex64) -> vis (device, complex64 or complex128); uncovered samples are 0
+p9idg_status ensure_gaps(p9idg_plan *p);
+
+// zero_gaps: zero only the visibilities no subgrid covers (the degridder writes every other one)
+// instead of the whole output -- for an output in host memory, where every byte crosses the link.
 p9idg_status run_degrid(p9idg_plan *p, const float2 *d_grid, bool grid_shifted, void *d_vis, bool out_c128,
-                        bool wstack) {
+                        bool wstack, bool zero_gaps = false) {
     const int S = p->c.subgrid_size;
     CK(p->d_subgrids.ensure(sizeof(float2) * S * S * std::max<size_t>(1, p->dsub.size())));
     {
@@ -445,7 +468,13 @@ p9idg_status run_degrid(p9idg_plan *p, const float2 *d_grid, bool grid_shifted, 
     {
         StageScope t(p, P9IDG_STAGE_DEGRIDDER);
         const size_t nvis = static_cast<size_t>(p->nbl) * p->nt * p->nch;
-        CK(cudaMemsetAsync(d_vis, 0, nvis * (out_c128 ? sizeof(double2) : sizeof(float2)), p->stream));
+        if (zero_gaps && out_c128) {
+            TRY(ensure_gaps(p));
+            CK(launch_zero_ranges(static_cast<double2 *>(d_vis), p->d_gaps.as<int64_t>(),
+                                  static_cast<int64_t>(p->gaps.size() / 2), p->stream));
+        } else {
+            CK(cudaMemsetAsync(d_vis, 0, nvis * (out_c128 ? sizeof(double2) : sizeof(float2)), p->stream));
+        }
         GridderArgs a = gridder_args(p);
         a.items = p->d_ditems.as<WorkItem>();
         a.nitems = static_cast<int32_t>(p->ditems.size());
@@ -487,11 +516,89 @@ p9idg_status layers_to_host(p9idg_plan *p, const float2 *d_layers, size_t count,
     return d2h(p, out, p->d_out128.p, sizeof(double2) * count);
 }
 
+// Uncovered visibility ranges (quirk P1 drops, baselines without subgrids), built once.
+p9idg_status ensure_gaps(p9idg_plan *p) {
+    if (p->gaps_ready) return P9IDG_OK;
+    p->gaps.clear();
+    std::vector<std::vector<std::pair<int32_t, int32_t>>> cov(std::max(0, p->nbl));
+    for (const auto &sg : p->subs)
+        if (sg.baseline_idx >= 0 && sg.baseline_idx < p->nbl)
+            cov[sg.baseline_idx].emplace_back(sg.time_sample_start, sg.time_sample_start + sg.time_sample_count);
+    const int64_t nch = p->nch;
+    for (int b = 0; b < p->nbl; b++) {
+        auto &v = cov[b];
+        std::sort(v.begin(), v.end());
+        int32_t t = 0;
+        for (const auto &r : v) {
+            const int32_t a = std::max(0, std::min(r.first, p->nt)), e = std::max(0, std::min(r.second, p->nt));
+            if (a > t) {
+                p->gaps.push_back((static_cast<int64_t>(b) * p->nt + t) * nch);
+                p->gaps.push_back(static_cast<int64_t>(a - t) * nch);
+            }
+            t = std::max(t, e);
+        }
+        if (t < p->nt) {
+            p->gaps.push_back((static_cast<int64_t>(b) * p->nt + t) * nch);
+            p->gaps.push_back(static_cast<int64_t>(p->nt - t) * nch);
+        }
+    }
+    // AdderWStack.Add's target layer of each subgrid it does not skip (AdderWStack.cs:41-51)
+    const int N = p->c.grid_size, S = p->c.subgrid_size, W = p->c.wlayer_count;
+    p->layer_used.assign(std::max(W, 1), 0);
+    for (const auto &sg : p->subs) {
+        int sx = sg.u_pixel, sy = sg.v_pixel, sw = sg.w_lambda;
+        if (sw < 0) {
+            sx = N - sx - S + 1;
+            sy = N - sy - S + 1;
+            sw = -sw - 1;
+        }
+        if (sx >= 1 && sx < N - S && sy >= 1 && sy < N - S && sw >= 0 && sw < W) p->layer_used[sw] = 1;
+    }
+    CK(p->d_gaps.ensure(sizeof(int64_t) * std::max<size_t>(2, p->gaps.size())));
+    if (!p->gaps.empty())
+        CK(cudaMemcpyAsync(p->d_gaps.p, p->gaps.data(), sizeof(int64_t) * p->gaps.size(), cudaMemcpyHostToDevice,
+                           p->stream));
+    CK(cudaStreamSynchronize(p->stream));
+    p->gaps_ready = true;
+    return P9IDG_OK;
+}
+
+bool host_in_place(const p9idg_plan *p) { return p->host_direct && p->host_access != 0; }
+
 p9idg_status host_grid_common(p9idg_plan *p, const double *vis, const double *uvw, double *out, bool wstack) {
     if (!p || !vis || !out) return fail(P9IDG_INVALID_ARGUMENT, "null argument");
     TRY(wstack ? check_wstack_layers(p) : check_adder_range(p));
     TRY(prepare(p, uvw));
     const size_t nvis = vis_count_of(p), nl = wstack ? p->c.wlayer_count : 1;
+    if (host_in_place(p)) {
+        // The gridder reads the caller's complex128 visibilities in host memory, once each, and the
+        // widening of the layers writes straight into the caller's output.  Layers no subgrid adds
+        // into are zeroed in the output at once, beside the gridder: those writes use the
+        // device-to-host direction of the link while the gridder's reads use the other.
+        const size_t nn = nn_of(p);
+        CK(p->d_layers.ensure(sizeof(float2) * nl * nn));
+        std::vector<char> used(nl, 1);
+        if (wstack) {
+            TRY(ensure_gaps(p));
+            used.assign(p->layer_used.begin(), p->layer_used.begin() + nl);
+        }
+        auto *out128 = reinterpret_cast<double2 *>(out);
+        CK(cudaEventRecord(p->ev_fork, p->stream));
+        CK(cudaStreamWaitEvent(p->side, p->ev_fork, 0));
+        for (size_t k = 0; k < nl; k++)
+            if (!used[k]) CK(launch_zero_c128(out128 + k * nn, static_cast<int64_t>(nn), p->side));
+        CK(cudaEventRecord(p->ev_join, p->side));
+        TRY(run_grid(p, vis, true, p->d_layers.as<float2>(), wstack));
+        {
+            StageScope t(p, P9IDG_STAGE_D2H);
+            for (size_t k = 0; k < nl; k++)
+                if (used[k])
+                    CK(launch_c64_to_c128(p->d_layers.as<float2>() + k * nn, static_cast<int64_t>(nn), out128 + k * nn,
+                                          p->stream));
+        }
+        CK(cudaStreamWaitEvent(p->stream, p->ev_join, 0));
+        return finish_call(p);
+    }
     CK(p->d_vis_in.ensure(sizeof(double2) * std::max<size_t>(1, nvis)));
     CK(p->d_layers.ensure(sizeof(float2) * nl * nn_of(p)));
     TRY(h2d(p, p->d_vis_in.p, vis, sizeof(double2) * nvis));
@@ -504,6 +611,24 @@ p9idg_status host_degrid_common(p9idg_plan *p, double *grid_io, const double *uv
     if (!p || !grid_io || !vis_out) return fail(P9IDG_INVALID_ARGUMENT, "null argument");
     TRY(prepare(p, uvw));
     const size_t nn = nn_of(p), nvis = vis_count_of(p);
+    if (host_in_place(p)) {
+        CK(p->d_grid128b.ensure(sizeof(double2) * nn));
+        CK(p->d_grid64.ensure(sizeof(float2) * nn));
+        {
+            StageScope t(p, P9IDG_STAGE_H2D);  // reads the caller's grid in host memory
+            CK(launch_shift_convert(reinterpret_cast<const double2 *>(grid_io), p->c.grid_size,
+                                    p->d_grid64.as<float2>(), p->d_grid128b.as<double2>(), p->stream));
+        }
+        // FFT.Shift(grid) mutates the caller's array (IDG.cs:24,44): copied back beside the degridder
+        CK(cudaEventRecord(p->ev_fork, p->stream));
+        CK(cudaStreamWaitEvent(p->side, p->ev_fork, 0));
+        CK(cudaMemcpyAsync(grid_io, p->d_grid128b.p, sizeof(double2) * nn, cudaMemcpyDeviceToHost, p->side));
+        CK(cudaEventRecord(p->ev_join, p->side));
+        // the degridder writes the caller's complex128 output in place; uncovered samples are zeroed
+        TRY(run_degrid(p, p->d_grid64.as<float2>(), true, vis_out, true, wstack, true));
+        CK(cudaStreamWaitEvent(p->stream, p->ev_join, 0));
+        return finish_call(p);
+    }
     CK(p->d_grid128.ensure(sizeof(double2) * nn));
     CK(p->d_grid128b.ensure(sizeof(double2) * nn));
     CK(p->d_grid64.ensure(sizeof(float2) * nn));
@@ -790,6 +915,19 @@ p9idg_status p9idg_plan_get_params(const p9idg_plan *plan, p9idg_params *out) {
     return P9IDG_OK;
 }
 
+p9idg_status p9idg_plan_set_host_access(p9idg_plan *plan, int32_t in_place) {
+    if (!plan) return fail(P9IDG_INVALID_ARGUMENT, "null plan");
+    plan->host_access = in_place != 0;
+    return P9IDG_OK;
+}
+
+p9idg_status p9idg_plan_get_host_access(p9idg_plan *plan, int32_t *in_place) {
+    if (!plan || !in_place) return fail(P9IDG_INVALID_ARGUMENT, "null argument");
+    TRY(ensure_device(plan));
+    *in_place = host_in_place(plan) ? 1 : 0;
+    return P9IDG_OK;
+}
+
 p9idg_status p9idg_plan_init_device(p9idg_plan *plan) {
     if (!plan) return fail(P9IDG_INVALID_ARGUMENT, "null plan");
     return ensure_device(plan);
@@ -812,6 +950,10 @@ void p9idg_plan_destroy(p9idg_plan *plan) {
         for (DevBuf *b : bufs) b->release();
         tc_release(plan->tc);
         plan->fft.release();
+        plan->d_gaps.release();
+        if (plan->side) cudaStreamDestroy(plan->side);
+        if (plan->ev_fork) cudaEventDestroy(plan->ev_fork);
+        if (plan->ev_join) cudaEventDestroy(plan->ev_join);
         if (plan->own_stream) cudaStreamDestroy(plan->own_stream);
     }
     delete plan;

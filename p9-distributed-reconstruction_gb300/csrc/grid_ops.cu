@@ -4,6 +4,8 @@
 // FFT.Backward, FFT.cs:159-185), plus the sincos throughput probe used as the FP32/SFU
 // roofline denominator.  All are grid-stride loops sized to the SM count.
 
+#include <algorithm>
+
 #include "kernels.cuh"
 
 namespace p9idg {
@@ -153,6 +155,35 @@ __global__ void fma_probe_kernel(int iters, float seed, float *sink) {
 
 cudaError_t launch_shift_convert(const double2 *in, int n, float2 *out64, double2 *out128, cudaStream_t st) {
     shift_convert_kernel<<<grid_blocks(static_cast<int64_t>(n) * n, 256), 256, 0, st>>>(in, n, out64, out128);
+    return cudaGetLastError();
+}
+
+// Zeroes the listed index ranges (pairs start, count) of a complex128 array.
+__global__ void zero_ranges_kernel(double2 *__restrict__ out, const int64_t *__restrict__ ranges, int64_t nranges) {
+    for (int64_t r = blockIdx.x; r < nranges; r += gridDim.x) {
+        const int64_t start = ranges[2 * r], count = ranges[2 * r + 1];
+        for (int64_t j = threadIdx.x; j < count; j += blockDim.x) out[start + j] = make_double2(0.0, 0.0);
+    }
+}
+
+__global__ void zero_c128_kernel(double2 *__restrict__ out, int64_t count) {
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < count;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+        out[i] = make_double2(0.0, 0.0);
+}
+
+// Few CTAs: this zero-fill of host memory is bound by the link and runs beside the gridder, which
+// should keep the SMs.
+cudaError_t launch_zero_c128(double2 *out, int64_t count, cudaStream_t st) {
+    if (count == 0) return cudaSuccess;
+    zero_c128_kernel<<<32, 512, 0, st>>>(out, count);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_zero_ranges(double2 *out, const int64_t *ranges, int64_t nranges, cudaStream_t st) {
+    if (nranges == 0) return cudaSuccess;
+    const unsigned blocks = static_cast<unsigned>(std::min<int64_t>(nranges, 8192));
+    zero_ranges_kernel<<<blocks, 256, 0, st>>>(out, ranges, nranges);
     return cudaGetLastError();
 }
 

@@ -99,6 +99,8 @@ cudaError_t launch_split_subgrid_fft(const SubgridOpArgs &a, cudaStream_t st, co
 // c128 (unshifted, host layout) -> c64 shifted copy and, when out128 != null, c128 shifted copy.
 cudaError_t launch_shift_convert(const double2 *in, int n, float2 *out64, double2 *out128, cudaStream_t st);
 cudaError_t launch_c64_to_c128(const float2 *in, int64_t count, double2 *out, cudaStream_t st);
+cudaError_t launch_zero_ranges(double2 *out, const int64_t *ranges, int64_t nranges, cudaStream_t st);
+cudaError_t launch_zero_c128(double2 *out, int64_t count, cudaStream_t st);
 cudaError_t launch_c128_to_c64(const double2 *in, int64_t count, float2 *out, cudaStream_t st);
 cudaError_t launch_unit_vis(const uint8_t *flags, int64_t count, float2 *out, cudaStream_t st);
 // sum over layers (c64 or c128 input) -> c64 grid

@@ -164,6 +164,16 @@ class Plan:
         t = None if taper is None else np.ascontiguousarray(taper, np.float32)
         _check(nat.lib().p9idg_plan_set_taper(self.handle, _ptr(t)))
 
+    def set_host_access(self, in_place: bool):
+        """Host-array calls use the caller's arrays in place (1, where the device reaches host
+        memory) or stage them through device copies (0)."""
+        _check(nat.lib().p9idg_plan_set_host_access(self.handle, int(bool(in_place))))
+
+    def host_access(self) -> bool:
+        v = ctypes.c_int32()
+        _check(nat.lib().p9idg_plan_get_host_access(self.handle, ctypes.byref(v)))
+        return bool(v.value)
+
     def set_stream(self, stream_handle: int):
         _check(nat.lib().p9idg_plan_set_stream(self.handle, ctypes.c_void_p(stream_handle or None)))
 
