@@ -334,6 +334,26 @@ p9idg_status p9idg_major_cycle_serial_cd_device(p9idg_plan *plan, const p9idg_mc
                                                 const uint8_t *d_flags, float *d_model, float *d_residual,
                                                 float *d_psf, p9idg_mc_cycle *cycles, int32_t *ncycles);
 
+/* ---------------- FITS input/output of the reference's data layout (Core/FitsIO.cs) ---------------- */
+/* Host-side, no GPU needed.  Primary-HDU arrays, big-endian; shapes are FITS axes (NAXIS1 first). */
+p9idg_status p9idg_fits_shape(const char *path, int32_t *bitpix, int32_t *naxis, int64_t *axes, int32_t max_axes);
+/* FitsIO.ReadUVW(file, fromBl, toBl) (FitsIO.cs:196-242): out double[to-from][nt][3], v negated. */
+p9idg_status p9idg_fits_read_uvw(const char *path, int32_t from_bl, int32_t to_bl, double *out);
+/* FitsIO.ReadFrequencies (FitsIO.cs:186-191). */
+p9idg_status p9idg_fits_read_frequencies(const char *path, double *out, int64_t capacity);
+/* FitsIO.ReadVisibilities(file, fromBl, toBl, nt, nch, norm) (FitsIO.cs:262-326): out complex128
+ * [to-from][nt][nch] = (XX + YY) / norm, from polarisations 0 and 3. */
+p9idg_status p9idg_fits_read_visibilities(const char *path, int32_t from_bl, int32_t to_bl, int32_t nt, int32_t nch,
+                                          double norm, double *out);
+/* FitsIO.ReadFlags(file, fromBl, toBl, nt, nch) (FitsIO.cs:328-389): out 1 byte each, 1 where the
+ * polarisation values sum to non-zero. */
+p9idg_status p9idg_fits_read_flags(const char *path, int32_t from_bl, int32_t to_bl, int32_t nt, int32_t nch,
+                                   uint8_t *out);
+/* FitsIO.ReadImage (bitpix -32, float) / ReadImageDouble (-64, double) (FitsIO.cs:140-185). */
+p9idg_status p9idg_fits_read_image(const char *path, int32_t bitpix, void *out, int64_t capacity);
+/* FitsIO.Write<T>(T[,] img) (FitsIO.cs:64-84), float (-32) or double (-64) [rows][cols]. */
+p9idg_status p9idg_fits_write_image(const char *path, int32_t bitpix, const void *data, int32_t rows, int32_t cols);
+
 /* ---------------- stage timing (CUDA events on the plan's stream) ---------------- */
 
 enum {

@@ -11,8 +11,9 @@ from ._native import (MODE_FP32, MODE_TC_BF16X3, MODE_TC_FP16X3, NativeLibraryMi
 from .idg import (FFT, IDG, Batch, GriddingConstants, P9IDGError, Partition, Partitioner, Plan, Subgrid, SUBGRID_DTYPE,
                   autotune, device_count, measure_sincos_peak, plan_from_subgrids, set_chunking)
 from .deconv import PSF, DeconvolutionResult, FastSerialCD, MajorCycle, PaddedConvolver, Rectangle
+from .fitsio import FitsIO
 
 __all__ = ["FFT", "IDG", "Batch", "autotune", "set_chunking", "GriddingConstants", "P9IDGError", "Partition", "Partitioner", "Plan", "Subgrid",
            "SUBGRID_DTYPE", "MODE_FP32", "MODE_TC_BF16X3", "MODE_TC_FP16X3", "NativeLibraryMissing", "STAGES",
            "device_count", "measure_sincos_peak", "plan_from_subgrids",
-           "PSF", "DeconvolutionResult", "FastSerialCD", "MajorCycle", "PaddedConvolver", "Rectangle"]
+           "PSF", "DeconvolutionResult", "FastSerialCD", "MajorCycle", "PaddedConvolver", "Rectangle", "FitsIO"]

@@ -129,6 +129,13 @@ SIGNATURES = {
     "p9idg_psf_amap": (i32, [P, i32, i32, i32, i32, P]),
     "p9idg_major_cycle_serial_cd": (i32, [P, P, P, P, P, P, P, P, ctypes.POINTER(i32)]),
     "p9idg_major_cycle_serial_cd_device": (i32, [P, P, P, P, P, P, P, P, ctypes.POINTER(i32)]),
+    "p9idg_fits_shape": (i32, [ctypes.c_char_p, ctypes.POINTER(i32), ctypes.POINTER(i32), P, i32]),
+    "p9idg_fits_read_uvw": (i32, [ctypes.c_char_p, i32, i32, P]),
+    "p9idg_fits_read_frequencies": (i32, [ctypes.c_char_p, P, i64]),
+    "p9idg_fits_read_visibilities": (i32, [ctypes.c_char_p, i32, i32, i32, i32, dbl, P]),
+    "p9idg_fits_read_flags": (i32, [ctypes.c_char_p, i32, i32, i32, i32, P]),
+    "p9idg_fits_read_image": (i32, [ctypes.c_char_p, i32, P, i64]),
+    "p9idg_fits_write_image": (i32, [ctypes.c_char_p, i32, P, i32, i32]),
 }
 
 _lib = None
