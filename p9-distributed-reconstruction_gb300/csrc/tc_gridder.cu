@@ -151,7 +151,7 @@ __global__ void tc_coef_kernel(const DevSubgrid *subs, const int64_t *coef_off, 
 // never wait on global memory.
 
 constexpr int kGVps = 32;      // visibilities per pipeline stage (K = 64)
-constexpr int kGStages = 3;
+constexpr int kGStages = 2;
 constexpr int kGProducerWarps = 8;
 constexpr int kGMmaWarp = 8;
 constexpr int kGLoaderWarp = 9;
@@ -165,7 +165,7 @@ constexpr uint32_t kGSmem = kGStages * kGStageBytes + kGRing * kGRingSlot + 512 
 constexpr uint32_t kGTmemCols = 64;
 
 template <bool BF16, typename VisT, bool BATCH>
-__global__ void __launch_bounds__(kGThreads, 2) tc_gridder_kernel(const TcArgs L, const TcArgs *__restrict__ probs) {
+__global__ void __launch_bounds__(kGThreads, 3) tc_gridder_kernel(const TcArgs L, const TcArgs *__restrict__ probs) {
     extern __shared__ unsigned char smem_raw[];
     unsigned char *smem = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     unsigned char *ring = smem + kGStages * kGStageBytes;
