@@ -217,6 +217,11 @@ p9idg_status p9idg_batch_degrid_w(p9idg_batch *batch);
 p9idg_status p9idg_batch_capture_graph(p9idg_batch *batch);
 /* grid_w then degrid_w (graph replay once captured). */
 p9idg_status p9idg_batch_run(p9idg_batch *batch);
+/* Launch order of the work items: THROUGHPUT (default) interleaves all problems largest item
+ * first; SMALL_FIRST runs the problems in order of size so the small ones finish early in each
+ * phase.  Drops a captured graph (capture again). */
+enum { P9IDG_SCHEDULE_THROUGHPUT = 0, P9IDG_SCHEDULE_SMALL_FIRST = 1 };
+p9idg_status p9idg_batch_set_schedule(p9idg_batch *batch, int32_t schedule);
 p9idg_status p9idg_batch_synchronize(p9idg_batch *batch);
 /* Per problem: ms from the start of the last degrid phase to the problem's last visibility (-1 if none). */
 p9idg_status p9idg_batch_latencies(p9idg_batch *batch, double *ms);

@@ -98,6 +98,7 @@ SIGNATURES = {
     "p9idg_batch_degrid_w": (i32, [P]),
     "p9idg_batch_capture_graph": (i32, [P]),
     "p9idg_batch_run": (i32, [P]),
+    "p9idg_batch_set_schedule": (i32, [P, i32]),
     "p9idg_batch_synchronize": (i32, [P]),
     "p9idg_batch_latencies": (i32, [P, P]),
     "p9idg_batch_get_stream": (i32, [P, ctypes.POINTER(P)]),

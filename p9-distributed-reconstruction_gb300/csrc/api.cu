@@ -714,6 +714,9 @@ struct p9idg_batch {
     DevBuf d_gargs, d_dargs, d_aargs, d_sargs, d_tg, d_td;  // per-problem argument tables
     DevBuf d_gitems, d_ditems, d_refs, d_done_init, d_done, d_finish, d_start;
     int32_t ngitems = 0, nditems = 0, nrefs = 0;
+    std::vector<WorkItem> h_gitems, h_ditems;  // merged work items of all problems, in launch order
+    std::vector<int64_t> prob_vis;             // visibilities per problem (for the schedules)
+    int32_t schedule = P9IDG_SCHEDULE_THROUGHPUT;
     std::vector<void *> layers, vis_out;
     std::vector<size_t> layer_bytes, vis_bytes;
     cudaGraph_t graph = nullptr;
@@ -776,6 +779,30 @@ template <typename T>
 p9idg_status upload(DevBuf &buf, const std::vector<T> &v) {
     CK(buf.ensure(sizeof(T) * std::max<size_t>(1, v.size())));
     if (!v.empty()) CK(cudaMemcpy(buf.p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice));
+    return P9IDG_OK;
+}
+
+// Launch order of the merged work items.  THROUGHPUT: largest item first across all problems
+// (the tail is short).  SMALL_FIRST: problems in order of size, each problem's items largest
+// first, so small problems finish early in each phase.
+p9idg_status batch_order(p9idg_batch *b, int32_t schedule) {
+    const auto &pv = b->prob_vis;
+    auto item_vis = [&](const WorkItem &w) { return static_cast<int64_t>(w.nt) * b->plans[w.problem]->nch; };
+    auto throughput = [&](const WorkItem &x, const WorkItem &y) { return item_vis(x) > item_vis(y); };
+    auto small_first = [&](const WorkItem &x, const WorkItem &y) {
+        if (x.problem != y.problem)
+            return pv[x.problem] != pv[y.problem] ? pv[x.problem] < pv[y.problem] : x.problem < y.problem;
+        return item_vis(x) > item_vis(y);
+    };
+    for (auto *v : {&b->h_gitems, &b->h_ditems}) {
+        if (schedule == P9IDG_SCHEDULE_SMALL_FIRST)
+            std::stable_sort(v->begin(), v->end(), small_first);
+        else
+            std::stable_sort(v->begin(), v->end(), throughput);
+    }
+    TRY(upload(b->d_gitems, b->h_gitems));
+    TRY(upload(b->d_ditems, b->h_ditems));
+    b->schedule = schedule;
     return P9IDG_OK;
 }
 
@@ -1321,23 +1348,38 @@ p9idg_status p9idg_batch_create(p9idg_plan *const *plans, int32_t nplans, const 
         cudaError_t e2 = cudaStreamSynchronize(p->stream);
         if (e2 != cudaSuccess) return bail(cuda_fail(e2, "plan preparation"));
     }
-    // one largest-first schedule across every problem
-    auto by_size = [&](const WorkItem &x, const WorkItem &y) {
-        return static_cast<int64_t>(x.nt) * plans[x.problem]->nch > static_cast<int64_t>(y.nt) * plans[y.problem]->nch;
-    };
-    std::stable_sort(gitems.begin(), gitems.end(), by_size);
-    std::stable_sort(ditems.begin(), ditems.end(), by_size);
-    b->ngitems = static_cast<int32_t>(gitems.size());
-    b->nditems = static_cast<int32_t>(ditems.size());
+    b->prob_vis.assign(nplans, 0);
+    for (const WorkItem &w : gitems) b->prob_vis[w.problem] += static_cast<int64_t>(w.nt) * plans[w.problem]->nch;
+    b->h_gitems = std::move(gitems);
+    b->h_ditems = std::move(ditems);
+    b->ngitems = static_cast<int32_t>(b->h_gitems.size());
+    b->nditems = static_cast<int32_t>(b->h_ditems.size());
     b->nrefs = static_cast<int32_t>(refs.size());
     if ((st = upload(b->d_gargs, ga)) != P9IDG_OK || (st = upload(b->d_dargs, da)) != P9IDG_OK ||
         (st = upload(b->d_aargs, aa)) != P9IDG_OK || (st = upload(b->d_sargs, sa)) != P9IDG_OK ||
         (st = upload(b->d_tg, tg)) != P9IDG_OK || (st = upload(b->d_td, td)) != P9IDG_OK ||
-        (st = upload(b->d_gitems, gitems)) != P9IDG_OK || (st = upload(b->d_ditems, ditems)) != P9IDG_OK ||
-        (st = upload(b->d_refs, refs)) != P9IDG_OK || (st = upload(b->d_done_init, done)) != P9IDG_OK)
+        (st = upload(b->d_refs, refs)) != P9IDG_OK || (st = upload(b->d_done_init, done)) != P9IDG_OK ||
+        (st = batch_order(b, P9IDG_SCHEDULE_THROUGHPUT)) != P9IDG_OK)
         return bail(st);
     *out = b;
     return P9IDG_OK;
+}
+
+p9idg_status p9idg_batch_set_schedule(p9idg_batch *b, int32_t schedule) {
+    if (!b) return fail(P9IDG_INVALID_ARGUMENT, "null batch");
+    if (schedule != P9IDG_SCHEDULE_THROUGHPUT && schedule != P9IDG_SCHEDULE_SMALL_FIRST)
+        return fail(P9IDG_INVALID_ARGUMENT, "unknown schedule");
+    CK(cudaSetDevice(b->device));
+    CK(cudaStreamSynchronize(b->stream));
+    if (b->exec) {  // the captured graph launches the old order's item count; capture again
+        cudaGraphExecDestroy(b->exec);
+        b->exec = nullptr;
+    }
+    if (b->graph) {
+        cudaGraphDestroy(b->graph);
+        b->graph = nullptr;
+    }
+    return batch_order(b, schedule);
 }
 
 p9idg_status p9idg_batch_grid_w(p9idg_batch *b) {

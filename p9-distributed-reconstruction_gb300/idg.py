@@ -438,6 +438,12 @@ class Batch:
     def run(self):
         _check(nat.lib().p9idg_batch_run(self._h))
 
+    THROUGHPUT, SMALL_FIRST = 0, 1
+
+    def set_schedule(self, schedule: int):
+        """Work-item order: Batch.THROUGHPUT (default) or Batch.SMALL_FIRST; drops a captured graph."""
+        _check(nat.lib().p9idg_batch_set_schedule(self._h, int(schedule)))
+
     def synchronize(self):
         _check(nat.lib().p9idg_batch_synchronize(self._h))
 

@@ -68,6 +68,29 @@ def test_batch_matches_single_plans(need_gpu, mode):
     batch.destroy()
 
 
+def test_small_first_schedule(need_gpu):
+    """The SMALL_FIRST order gives the same results and finishes the smallest problem first."""
+    torch = pytest.importorskip("torch")
+    probs = _problems(torch, pkg.MODE_TC_BF16X3)
+    batch = pkg.Batch([p.plan for p, _, _ in probs], [b["vis"].data_ptr() for _, _, b in probs],
+                      [b["layers"].data_ptr() for _, _, b in probs], [b["grid"].data_ptr() for _, _, b in probs],
+                      [b["out"].data_ptr() for _, _, b in probs])
+    batch.run()
+    batch.synchronize()
+    ref = [(b["layers"].cpu().numpy(), b["out"].cpu().numpy()) for _, _, b in probs]
+    batch.set_schedule(pkg.Batch.SMALL_FIRST)
+    batch.capture_graph()
+    batch.run()
+    batch.synchronize()
+    for (_, _, b), (lay, vo) in zip(probs, ref):
+        assert rel_l2(b["layers"].cpu().numpy(), lay) < 1e-6
+        assert rel_l2(b["out"].cpu().numpy(), vo) < 1e-6
+    sizes = [p.plan.info()["gridded_visibilities"] for p, _, _ in probs]
+    lat = batch.latencies_ms()
+    assert lat[int(np.argmin(sizes))] <= lat[int(np.argmax(sizes))]
+    batch.destroy()
+
+
 def test_batch_rejects_mixed_subgrid_sizes(need_gpu):
     torch = pytest.importorskip("torch")
     obs, cd = synth.build(synth.scaled_workload("small_256", n_ant=5, nt=50, nch=4))
