@@ -133,6 +133,10 @@ p9idg_status p9idg_plan_get_host_access(p9idg_plan *plan, int32_t *in_place);
 void p9idg_plan_destroy(p9idg_plan *plan);
 
 /* ---------------- IDG facade, host arrays (Core/ImageDomainGridder/IDG.cs) ---------------- */
+/* Every array is sized from the plan (vis and flags [nbl][nt][nch], uvw [nbl][nt][3], grids
+ * [N][N], layers [W][N][N]) and must hold that many elements: the library cannot see the
+ * caller's array bounds, and with in-place host access (p9idg_plan_set_host_access) the kernels
+ * read and write the arrays themselves.  The P/Invoke shim checks GetLength() against the plan. */
 /* uvw may be NULL to reuse the uvw the plan was created with. */
 
 /* IDG.Grid (IDG.cs:12-20): Gridder.Forward, SubgridFFT.Forward, Adder.Add, FFT.Shift.  grid_out Complex[N,N]. */

@@ -15,7 +15,7 @@ import dataclasses
 import numpy as np
 
 from . import _native as nat
-from .idg import GriddingConstants, P9IDGError, _check, _plan_for, _ptr
+from .idg import GriddingConstants, P9IDGError, _check, _check_inputs, _plan_for, _ptr
 
 MAJOR_EPSILON = 1e-4  # MajorCycle.cs:18 (1e-4f)
 
@@ -100,9 +100,16 @@ class FastSerialCD:
         _check(nat.lib().p9idg_cd_get_maps(self._h, _ptr(psf2), _ptr(amap)))
         return psf2, amap
 
+    def _images(self, x, g, writable):
+        x, g = _f32(x, writable), _f32(g, writable)
+        for a, name in ((x, "xImage"), (g, "bMap")):
+            if a.shape != (self.n, self.n):
+                raise ValueError(f"{name} has shape {a.shape}; the deconvolver's image is {(self.n, self.n)}")
+        return x, g
+
     def Deconvolve(self, xImage, bMap, lambda_, alpha, maxIteration, epsilon=1e-4) -> DeconvolutionResult:
         """Updates xImage and bMap (float32, C-contiguous) in place, as the reference does."""
-        x, g = _f32(xImage, True), _f32(bMap, True)
+        x, g = self._images(xImage, bMap, True)
         r = _CdResult()
         _check(nat.lib().p9idg_cd_deconvolve(self._h, _ptr(x), _ptr(g), float(lambda_), float(alpha), int(maxIteration),
                                              float(epsilon), ctypes.byref(r)))
@@ -117,7 +124,7 @@ class FastSerialCD:
 
     def DeconvolvePath(self, xImage, bMap, lambdaMin, lambdaFactor, alpha, maxPathIteration=10, maxIteration=100,
                        epsilon=1e-4) -> DeconvolutionResult:
-        x, g = _f32(xImage, True), _f32(bMap, True)
+        x, g = self._images(xImage, bMap, True)
         r = _CdResult()
         _check(nat.lib().p9idg_cd_deconvolve_path(self._h, _ptr(x), _ptr(g), float(lambdaMin), float(lambdaFactor),
                                                   float(alpha), int(maxPathIteration), int(maxIteration),
@@ -125,7 +132,7 @@ class FastSerialCD:
         return DeconvolutionResult(bool(r.converged), r.iterations, r.elapsed_ms)
 
     def GetAbsMaxDiff(self, xImage, gradients, lambda_, alpha) -> float:
-        x, g = _f32(xImage), _f32(gradients)
+        x, g = self._images(xImage, gradients, False)
         v = ctypes.c_float()
         _check(nat.lib().p9idg_cd_get_abs_max_diff(self._h, _ptr(x), _ptr(g), float(lambda_), float(alpha),
                                                    ctypes.byref(v)))
@@ -257,8 +264,7 @@ class MajorCycle:
         plan = _plan_for(c, metadata, uvw, frequencies)
         vis = np.ascontiguousarray(visibilities, np.complex128)
         fl = np.ascontiguousarray(flags, np.uint8)
-        if fl.shape != vis.shape:
-            raise ValueError("flags must have the visibilities' shape")
+        _check_inputs(plan, c, vis=vis, uvw=uvw, flags=fl)
         N = c.GridSize
         model = np.zeros((N, N), np.float32)
         resid = np.zeros((N, N), np.float32)

@@ -65,6 +65,20 @@ def _out(out, shape):
     return out
 
 
+def _expect_shape(a, shape, name):
+    """The C ABI sizes every array from the plan; a wrong shape would be read or written out of
+    bounds, so it is refused here (the reference throws IndexOutOfRangeException)."""
+    if a is not None and tuple(np.shape(a)) != tuple(shape):
+        raise ValueError(f"{name} has shape {tuple(np.shape(a))}; the plan needs {tuple(shape)}")
+
+
+def _check_inputs(p, c, vis=None, uvw=None, flags=None, grid=None):
+    _expect_shape(vis, (p.nbl, p.nt, p.nch), "visibilities")
+    _expect_shape(uvw, (p.nbl, p.nt, 3), "uvw")
+    _expect_shape(flags, (p.nbl, p.nt, p.nch), "flags")
+    _expect_shape(grid, (c.GridSize, c.GridSize), "grid")
+
+
 class GriddingConstants:
     """Immutable gridding parameters (GriddingConstants.cs:11-52).
 
@@ -290,6 +304,7 @@ class IDG:
     def Grid(c, metadata, visibilities, uvw, frequencies, out=None) -> np.ndarray:
         p = _plan_for(c, metadata, uvw, frequencies)
         vis, uvw = _c128(visibilities, "visibilities"), _f64(uvw)
+        _check_inputs(p, c, vis=vis, uvw=uvw)
         out = _out(out, (c.GridSize, c.GridSize))
         _check(nat.lib().p9idg_grid(p.handle, _ptr(vis), _ptr(uvw), _ptr(out)))
         return out
@@ -306,6 +321,7 @@ class IDG:
         page-locked memory; the reference returns a new List<Complex[,]>."""
         p = _plan_for(c, metadata, uvw, frequencies)
         vis, uvw = _c128(visibilities, "visibilities"), _f64(uvw)
+        _check_inputs(p, c, vis=vis, uvw=uvw)
         out = _out(out, (c.WLayerCount, c.GridSize, c.GridSize))
         _check(nat.lib().p9idg_grid_w(p.handle, _ptr(vis), _ptr(uvw), _ptr(out)))
         return out
@@ -320,6 +336,7 @@ class IDG:
         g = grid if (isinstance(grid, np.ndarray) and grid.dtype == np.complex128 and grid.flags.c_contiguous
                      and grid.flags.writeable) else _c128(grid, "grid").copy()
         uvw = _f64(uvw)
+        _check_inputs(p, c, uvw=uvw, grid=g)
         vis = _out(out, (p.nbl, p.nt, p.nch))
         _check(fn(p.handle, _ptr(g), _ptr(uvw), _ptr(vis)))
         return vis
@@ -329,6 +346,7 @@ class IDG:
         p = _plan_for(c, metadata, uvw, frequencies)
         f = np.ascontiguousarray(flags, dtype=np.uint8)
         uvw = _f64(uvw)
+        _check_inputs(p, c, uvw=uvw, flags=f)
         out = np.empty((c.GridSize, c.GridSize), np.complex128)
         _check(nat.lib().p9idg_grid_psf(p.handle, _ptr(uvw), _ptr(f), _ptr(out)))
         return out
@@ -337,6 +355,7 @@ class IDG:
     def ToImage(c, metadata, visibilities, uvw, frequencies) -> np.ndarray:
         p = _plan_for(c, metadata, uvw, frequencies)
         vis, uvw = _c128(visibilities, "visibilities"), _f64(uvw)
+        _check_inputs(p, c, vis=vis, uvw=uvw)
         out = np.empty((c.GridSize, c.GridSize), np.float64)
         _check(nat.lib().p9idg_to_image(p.handle, _ptr(vis), _ptr(uvw), _ptr(out)))
         return out
@@ -346,6 +365,7 @@ class IDG:
         p = _plan_for(c, metadata, uvw, frequencies)
         f = np.ascontiguousarray(flags, dtype=np.uint8)
         uvw = _f64(uvw)
+        _check_inputs(p, c, uvw=uvw, flags=f)
         out = np.empty((c.GridSize, c.GridSize), np.float64)
         _check(nat.lib().p9idg_calculate_psf(p.handle, _ptr(uvw), _ptr(f), _ptr(out)))
         return out

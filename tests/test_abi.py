@@ -77,3 +77,21 @@ def test_adder_range_error_matches_reference():
         subs = oracle.partition(cd, uvw, freq)
         oracle.idg_grid(cd, subs, np.ones((1, 1, 1), np.complex128), uvw, freq)
     assert e2.value.code == 4
+
+
+def test_host_api_refuses_wrong_shapes():
+    """Every array is sized from the plan in the C ABI, so the Python mirror refuses arrays of
+    another shape instead of letting them be read or written out of bounds."""
+    from conftest import constants, workload
+    obs, cd = workload("small_256", n_ant=5, nt=20, nch=4)
+    c, cd = constants(cd)
+    part = pkg.Partitioner.CreatePartition(c, obs.uvw, obs.frequencies)
+    N = cd["grid_size"]
+    with pytest.raises(ValueError):
+        pkg.IDG.DeGridW(c, part, np.zeros((N // 2, N // 2), np.complex128), obs.uvw, obs.frequencies)
+    with pytest.raises(ValueError):
+        pkg.IDG.GridW(c, part, obs.vis[:, :10], obs.uvw, obs.frequencies)
+    with pytest.raises(ValueError):
+        pkg.IDG.CalculatePSF(c, part, obs.uvw, np.zeros((1, 1, 1), bool), obs.frequencies)
+    with pytest.raises((ValueError, pkg.P9IDGError)):  # a plan for other uvw dimensions is refused too
+        pkg.IDG.Grid(c, part, obs.vis, obs.uvw[:, :5], obs.frequencies)

@@ -172,25 +172,29 @@ def _mc_inputs():
 MC_ARGS = dict(psfCutFactor=8, maxMajorCycle=3, lambda_=0.5, alpha=0.05, deconvIterations=2000, deconvEpsilon=1e-5)
 
 
-def _run_gpu_mc(obs, c, mode):
+def _run_gpu_mc(obs, c, mode, flags=None):
     part = pkg.Partitioner.CreatePartition(c, obs.uvw, obs.frequencies)
     part.plan.set_mode(mode)
-    flags = np.zeros(obs.vis.shape, bool)
+    if flags is None:
+        flags = np.zeros(obs.vis.shape, bool)
     return pkg.MajorCycle.ReconstructSerialCD(c, part, obs.vis, obs.uvw, obs.frequencies, flags, **MC_ARGS)
 
 
-def test_major_cycle_vs_oracle(need_gpu):
+@pytest.mark.parametrize("flag_fraction", [0.0, 0.1], ids=["unflagged", "flagged"])
+def test_major_cycle_vs_oracle(need_gpu, flag_fraction):
     """MajorCycle.ReconstructSerialCD with the FP32 gridder vs the FP64 oracle loop: the same
     number of cycles and decisions, PSF and first dirty image to FP32-gridder accuracy, and the
     final model and residual within 1e-3 relative L2 (the CD sequence depends on gradients that
-    differ at ~1e-6 between the FP32 and FP64 gridders)."""
+    differ at ~1e-6 between the FP32 and FP64 gridders).  With flags, the PSF uses unit
+    visibilities only where unflagged, the first cycle grids the raw visibilities (flagged ones
+    included, as MajorCycle.cs:83,88 does) and later cycles the flag-zeroed residuals."""
     obs, c, cd = _mc_inputs()
     subs = oracle.partition(cd, obs.uvw, obs.frequencies)
-    flags = np.zeros(obs.vis.shape, np.uint8)
+    flags = (np.random.default_rng(12).random(obs.vis.shape) < flag_fraction).astype(np.uint8)
     ref = oracle.major_cycle(cd, subs, obs.uvw, obs.frequencies, obs.vis, flags, MC_ARGS["psfCutFactor"],
                              MC_ARGS["maxMajorCycle"], MC_ARGS["lambda_"], MC_ARGS["alpha"],
                              MC_ARGS["deconvIterations"], MC_ARGS["deconvEpsilon"])
-    got = _run_gpu_mc(obs, c, pkg.MODE_FP32)
+    got = _run_gpu_mc(obs, c, pkg.MODE_FP32, flags.astype(bool))
     cyc, rc = got["cycles"], ref["cycles"]
     assert len(cyc) == len(rc)
     assert [x["deconvolved"] for x in cyc] == list(rc["deconvolved"])

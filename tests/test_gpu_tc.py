@@ -76,3 +76,45 @@ def test_tc_rejects_other_subgrid_sizes():
     with pytest.raises(pkg.P9IDGError) as e:
         part.plan.set_mode(pkg.MODE_TC_BF16X3)
     assert e.value.code == 8
+
+
+@pytest.mark.parametrize("mode", MODES)
+@pytest.mark.parametrize("nch,nt,N,chunks", [
+    (1, 37, 256, None),       # one channel: work items far from a multiple of the 32 / 128 tiles
+    (3, 301, 255, None),      # odd grid size, odd channel count
+    (16, 120, 512, (2048, 2048)),  # small work items: several partial subgrids per subgrid
+])
+def test_tc_edge_shapes(need_gpu, mode, nch, nt, N, chunks):
+    obs, cd = workload("small_256", n_ant=9, nt=nt, nch=nch, seed=nch * 100 + nt)
+    c, cd = constants(cd, grid_size=N)
+    part = pkg.Partitioner.CreatePartition(c, obs.uvw, obs.frequencies)
+    part.plan.set_mode(mode)
+    if chunks:
+        pkg.set_chunking(part.plan, *chunks)
+    subs = oracle.partition(cd, obs.uvw, obs.frequencies)
+    assert len(subs) > 0
+    got = pkg.IDG.GridW(c, part, obs.vis, obs.uvw, obs.frequencies)
+    assert rel_l2(got, oracle.idg_grid_w(cd, subs, obs.vis, obs.uvw, obs.frequencies)) < TOL_TC
+    rng = np.random.default_rng(N)
+    model = rng.standard_normal((N, N)) + 1j * rng.standard_normal((N, N))  # the plan's grid size
+    vis = pkg.IDG.DeGridW(c, part, model.copy(), obs.uvw, obs.frequencies)
+    ref, _ = oracle.idg_degrid(cd, subs, model, obs.uvw, obs.frequencies, wstack=True)
+    assert rel_l2(vis, ref) < TOL_TC
+
+
+@pytest.mark.parametrize("mode", MODES)
+def test_tc_unit_delta_known_answer(need_gpu, mode):
+    """The hand-derived known answer of the FP32 path (a unit visibility at integer uv pixel p
+    grids to 1 at grid[p]) holds for the tensor-core path to its stated bound."""
+    from conftest import C_LIGHT, kat_constants
+    for pu, pv in [(0, 0), (3, -5), (11, 9)]:
+        cd = kat_constants(N=128, S=32, kernel=8)
+        c, cd = constants(cd)
+        uvw = np.array([[[pu, pv, 0.0]]], np.float64)
+        freq = np.array([C_LIGHT])
+        part = pkg.Partitioner.CreatePartition(c, uvw, freq)
+        part.plan.set_mode(mode)
+        g = pkg.IDG.Grid(c, part, np.ones((1, 1, 1), np.complex128), uvw, freq)
+        expect = np.zeros_like(g)
+        expect[pv % 128, pu % 128] = 1.0
+        assert np.abs(g - expect).max() < 1e-4
