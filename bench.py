@@ -540,6 +540,26 @@ def main():
     stages = head["stages"]
     launches = sum(n for (_, n) in stages.values()) - stages["h2d"][1] - stages["d2h"][1]
 
+    # tensor-core vs FP32 kernels on the whole workload: w layers, degridded visibilities, dirty image
+    tc_vs_fp32 = None
+    if compare:
+        outs = {}
+        for mode in ("fp32", headline):
+            plan.set_mode(MODES[mode])
+            step()
+            plan.wstack_image_device(d_layers.data_ptr(), d_img.data_ptr(), True)
+            plan.synchronize()
+            outs[mode] = (d_layers.clone(), d_out.clone(), d_img.clone())
+
+        def rel_dev(a, b):
+            return float(torch.linalg.vector_norm(a - b) / torch.linalg.vector_norm(b))
+
+        a, b = outs[headline], outs["fp32"]
+        tc_vs_fp32 = {"grid_w": rel_dev(a[0], b[0]), "degrid_w": rel_dev(a[1], b[1]),
+                      "dirty_image": rel_dev(a[2], b[2]), "visibilities": int(gridded)}
+        del outs, a, b
+        plan.set_mode(MODES[headline])
+
     # the full-grid w-layer FFT (FFT.WStackIFFTFloat + FFT.Shift), timed separately
     plan.reset_timing()
     plan.enable_timing(True)
@@ -650,6 +670,7 @@ def main():
                "modes": modes,
                "tc_over_fp32": (head["value"] / results["fp32"]["value"]) if "fp32" in results and
                headline != "fp32" else None,
+               "rel_l2_tc_vs_fp32_full_workload": tc_vs_fp32,
                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
                "clocks": head["clk"]}
         print(json.dumps(out), flush=True)
