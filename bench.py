@@ -84,6 +84,24 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.rows)}
 
 
+def gpu_local_cpus(gpu_index):
+    """Host CPUs on the GPU's own NUMA node (sysfs local_cpulist of its PCI function), or None."""
+    try:
+        bus = subprocess.run(["nvidia-smi", "--query-gpu=pci.bus_id", "--format=csv,noheader", "-i", str(gpu_index)],
+                             capture_output=True, text=True, timeout=20).stdout.strip()
+        dom, rest = bus.split(":", 1)
+        path = f"/sys/bus/pci/devices/{int(dom, 16):04x}:{rest.lower()}/local_cpulist"
+        cpus = set()
+        with open(path) as f:
+            for part in f.read().strip().split(","):
+                a, _, b = part.partition("-")
+                cpus.update(range(int(a), int(b or a) + 1))
+        cpus &= os.sched_getaffinity(0)
+        return cpus or None
+    except (OSError, ValueError, subprocess.SubprocessError):
+        return None
+
+
 def measured_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -598,6 +616,12 @@ def main():
     # e2e through the reference-facing host API (IDG.GridW + IDG.DeGridW) with pinned host buffers
     e2e = None
     if not args.no_e2e:
+        # the host arrays live on the GPU's NUMA node, as a deployment would place them: allocated
+        # and first touched by this thread while it runs on that node's CPUs
+        all_cpus = os.sched_getaffinity(0)
+        local_cpus = gpu_local_cpus(local)
+        if local_cpus:
+            os.sched_setaffinity(0, local_cpus)
         pin = lambda shape, dt: torch.empty(shape, dtype=dt, pin_memory=True).numpy()  # noqa: E731
         h_vis = pin(obs.vis.shape, torch.complex128)
         h_vis[...] = obs.vis
@@ -606,17 +630,25 @@ def main():
         h_grid = pin((N, N), torch.complex128)
         h_grid[...] = model_grid
         h_layers = pin((W, N, N), torch.complex128)
+        h_layers[...] = 0
         h_vout = pin(obs.vis.shape, torch.complex128)
+        h_vout[...] = 0
         plan.set_mode(MODES[headline])
         plan.set_stream(0)
         pkg.IDG.GridW(c, part, h_vis, h_uvw, obs.frequencies, out=h_layers)  # warm-up of the host path
         pkg.IDG.DeGridW(c, part, h_grid, h_uvw, obs.frequencies, out=h_vout)
         steps_e2e = max(1, min(args.steps, 5))
+        t_grid = t_degrid = 0.0
         t0 = time.perf_counter()
         for _ in range(steps_e2e):
+            ta = time.perf_counter()
             pkg.IDG.GridW(c, part, h_vis, h_uvw, obs.frequencies, out=h_layers)
+            tb = time.perf_counter()
             pkg.IDG.DeGridW(c, part, h_grid, h_uvw, obs.frequencies, out=h_vout)
+            t_grid += tb - ta
+            t_degrid += time.perf_counter() - tb
         t_e2e = time.perf_counter() - t0
+        os.sched_setaffinity(0, all_cpus)
         nvis = obs.vis.size
         h2d = nvis * 16 + 2 * obs.uvw.nbytes + N * N * 16
         d2h = W * N * N * 16 + N * N * 16 + nvis * 16
@@ -624,6 +656,8 @@ def main():
         e2e = {"value": ws * 2 * gridded * steps_e2e / t_e2e / 1e6, "unit": "Mvis/s",
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                "host_arrays_in_place": in_place,
+               "grid_w_ms": 1e3 * t_grid / steps_e2e, "degrid_w_ms": 1e3 * t_degrid / steps_e2e,
+               "host_numa_local_cpus": len(local_cpus) if local_cpus else None,
                "note": "IDG.GridW + IDG.DeGridW host API, Complex(double) arrays in pinned host memory, "
                        "wall clock incl. every host<->device transfer and complex128<->complex64 conversion"
                        + ("; the kernels read the visibilities and the model grid and write the degridded "
