@@ -66,9 +66,13 @@ p9idg_status cuda_fail(cudaError_t e, const char *what) {
         if (r_ != CUFFT_SUCCESS) return fail(P9IDG_CUDA_ERROR, std::string(#x) + " failed"); \
     } while (0)
 
-struct Buf {
+struct Buf {  // device buffer, freed when it goes out of scope (every early return included)
     void *p = nullptr;
     size_t bytes = 0;
+    Buf() = default;
+    Buf(const Buf &) = delete;
+    Buf &operator=(const Buf &) = delete;
+    ~Buf() { release(); }
     cudaError_t ensure(size_t n) {
         if (n <= bytes && p) return cudaSuccess;
         if (p) cudaFree(p);
