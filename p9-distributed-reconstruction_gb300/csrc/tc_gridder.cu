@@ -27,6 +27,7 @@
 //   MMA1: A_hi x B rows 64-191 (N128) -> cols 0..127 = [T0 | T1];  MMA2: A_hi x B0_lo (N64),
 //   MMA3: A_lo x B0_hi (N64) -> cols 0..63.  Two accumulators alternate (256 columns).
 
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
@@ -45,6 +46,15 @@ using namespace tc;
 
 constexpr int kS = 32;
 constexpr uint64_t kWaitNs = 2000000000ull;  // 2 s per wait before a kernel gives up
+
+// Tensor maps for TMA staging (single-plan launches with complex64 visibilities in device
+// memory): coefficients as a [ncoef][4] float32 tensor, visibilities as a [nvis] 64-bit tensor
+// read 34 at a time from an even index (the TMA x coordinate must be 16-byte aligned).
+struct TmaMaps {
+    CUtensorMap coef;
+    CUtensorMap vis;
+};
+constexpr int kVisBox = 34;
 
 // ---------------- bf16 / fp16 splitting ----------------
 
@@ -164,8 +174,9 @@ constexpr uint32_t kGStageBytes = kGStageA + kGStageB;
 constexpr uint32_t kGSmem = kGStages * kGStageBytes + kGRing * kGRingSlot + 512 + 1024;
 constexpr uint32_t kGTmemCols = 64;
 
-template <bool BF16, typename VisT, bool BATCH>
-__global__ void __launch_bounds__(kGThreads, 3) tc_gridder_kernel(const TcArgs L, const TcArgs *__restrict__ probs) {
+template <bool BF16, typename VisT, bool BATCH, bool TMA>
+__global__ void __launch_bounds__(kGThreads, 3)
+    tc_gridder_kernel(const TcArgs L, const TcArgs *__restrict__ probs, const __grid_constant__ TmaMaps maps) {
     extern __shared__ unsigned char smem_raw[];
     unsigned char *smem = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     unsigned char *ring = smem + kGStages * kGStageBytes;
@@ -186,8 +197,10 @@ __global__ void __launch_bounds__(kGThreads, 3) tc_gridder_kernel(const TcArgs L
     const int nvis = it.nt * g.nch;
     const int nstages = (nvis + kGVps - 1) / kGVps;
     // an item is a run of whole time samples: its visibilities and coefficients are contiguous
-    const VisT *vrow = static_cast<const VisT *>(a.vis) + (static_cast<int64_t>(sg.bl) * g.nt_all + it.t0) * g.nch;
-    const float4 *crow = a.coef + a.coef_off[it.subgrid] + static_cast<int64_t>(it.t0 - sg.t0) * g.nch;
+    const int64_t v0 = (static_cast<int64_t>(sg.bl) * g.nt_all + it.t0) * g.nch;  // first visibility
+    const int64_t c0 = a.coef_off[it.subgrid] + static_cast<int64_t>(it.t0 - sg.t0) * g.nch;
+    const VisT *vrow = static_cast<const VisT *>(a.vis) + v0;
+    const float4 *crow = a.coef + c0;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < kGStages; s++) {
@@ -195,7 +208,7 @@ __global__ void __launch_bounds__(kGThreads, 3) tc_gridder_kernel(const TcArgs L
             mbar_init(&empty[s], 1);
         }
         for (int s = 0; s < kGRing; s++) {
-            mbar_init(&in_full[s], 32);                  // one cp.async arrival per loader lane
+            mbar_init(&in_full[s], TMA ? 1 : 32);  // one expect_tx arrival, or one cp.async arrival per lane
             mbar_init(&in_empty[s], kGProducerWarps);
         }
         mbar_init(accb, 1);
@@ -238,6 +251,31 @@ __global__ void __launch_bounds__(kGThreads, 3) tc_gridder_kernel(const TcArgs L
             mma_commit(accb);
             // the MMAs must be finished before the TMEM is released
             if (!mbar_wait(accb, 0, abort_flag, kWaitNs)) atomicOr(a.status, kStatusWait);
+        }
+        __syncwarp();
+    } else if (warp == kGLoaderWarp && TMA) {
+        // ---- loader (TMA): stage i's 32 coefficients (one 2-D tile) and 34 visibilities from the
+        // even index at or below the stage's first (one 1-D tile) -> ring slot i % kGRing
+        if (lane == 0) {
+            int issued = 0;
+            for (int i = 0; i < nstages; i++) {
+                const int slot = i % kGRing;
+                const uint32_t ph = (i / kGRing) & 1;
+                if (!mbar_wait(&in_empty[slot], ph ^ 1, abort_flag, kWaitNs)) {
+                    *abort_flag = 1;
+                    atomicOr(a.status, kStatusWait);
+                    break;
+                }
+                const uint32_t dst = rbase + slot * kGRingSlot;
+                mbar_expect_tx(&in_full[slot], kGVps * 16 + kVisBox * 8);
+                tma_load_2d(dst, &maps.coef, 0, static_cast<int32_t>(c0 + i * kGVps), &in_full[slot]);
+                tma_load_1d(dst + 512, &maps.vis, static_cast<int32_t>((v0 + i * kGVps) & ~int64_t(1)), &in_full[slot]);
+                issued = i + 1;
+            }
+            // tiles still in flight land before the CTA can exit (consumed ones have completed)
+            volatile int never = 0;
+            for (int i = issued > kGRing ? issued - kGRing : 0; i < issued; i++)
+                if (!mbar_wait(&in_full[i % kGRing], (i / kGRing) & 1, &never, kWaitNs)) atomicOr(a.status, kStatusWait);
         }
         __syncwarp();
     } else if (warp == kGLoaderWarp) {
@@ -299,11 +337,14 @@ __global__ void __launch_bounds__(kGThreads, 3) tc_gridder_kernel(const TcArgs L
             float2 vv[4];
             {
                 const float4 *rc = reinterpret_cast<const float4 *>(ring + slot * kGRingSlot) + group * 4;
-                const VisT *rv = reinterpret_cast<const VisT *>(ring + slot * kGRingSlot + 512) + group * 4;
+                const int off = TMA ? static_cast<int>((v0 + i * kGVps) & 1) : 0;
+                const VisT *rv = reinterpret_cast<const VisT *>(ring + slot * kGRingSlot + 512) + off + group * 4;
 #pragma unroll
                 for (int v = 0; v < 4; v++) {
                     c[v] = rc[v];
                     vv[v] = load_vis(rv, v);
+                    // a TMA tile past the item's end holds the next item's samples: weight them 0
+                    if (TMA && i * kGVps + group * 4 + v >= nvis) vv[v] = make_float2(0.f, 0.f);
                 }
             }
             __syncwarp();
@@ -408,8 +449,9 @@ constexpr uint32_t kDTileBytes = 2 * kDTileHalf;
 constexpr uint32_t kDSmem = kDStatic + 2 * kDTileBytes + kDRing * kDRingSlot + 256 + 512 + 1024;
 constexpr uint32_t kDTmemCols = 256;
 
-template <bool BF16, typename OutT, bool BATCH>
-__global__ void __launch_bounds__(kDThreads, 2) tc_degridder_kernel(const TcArgs L, const TcArgs *__restrict__ probs) {
+template <bool BF16, typename OutT, bool BATCH, bool TMA>
+__global__ void __launch_bounds__(kDThreads, 2)
+    tc_degridder_kernel(const TcArgs L, const TcArgs *__restrict__ probs, const __grid_constant__ TmaMaps maps) {
     extern __shared__ unsigned char smem_raw[];
     unsigned char *smem = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     unsigned char *bstat = smem;
@@ -434,7 +476,8 @@ __global__ void __launch_bounds__(kDThreads, 2) tc_degridder_kernel(const TcArgs
     const DevSubgrid sg = a.subs[it.subgrid];
     const int nvis = it.nt * g.nch;
     const int ntiles = (nvis + kDTile - 1) / kDTile;
-    const float4 *crow = a.coef + a.coef_off[it.subgrid] + static_cast<int64_t>(it.t0 - sg.t0) * g.nch;
+    const int64_t c0 = a.coef_off[it.subgrid] + static_cast<int64_t>(it.t0 - sg.t0) * g.nch;
+    const float4 *crow = a.coef + c0;
 
     if (threadIdx.x == 0) {
         for (int b = 0; b < 2; b++) {
@@ -444,7 +487,7 @@ __global__ void __launch_bounds__(kDThreads, 2) tc_degridder_kernel(const TcArgs
             mbar_init(&acc_empty[b], 4);
         }
         for (int s = 0; s < kDRing; s++) {
-            mbar_init(&in_full[s], 32);  // one cp.async arrival per loader lane
+            mbar_init(&in_full[s], TMA ? 1 : 32);  // one expect_tx arrival, or one cp.async arrival per lane
             mbar_init(&in_empty[s], 8);  // 4 producer + 4 epilogue warps read each slot
         }
         *abort_flag = 0;
@@ -536,6 +579,29 @@ __global__ void __launch_bounds__(kDThreads, 2) tc_degridder_kernel(const TcArgs
             }
             // drain: every issued MMA finished before the TMEM is released
             mma_commit(&a_empty[0]);
+        }
+        __syncwarp();
+    } else if (warp == kDLoaderWarp && TMA) {
+        // ---- loader (TMA): tile i's 128 coefficients as one 2-D tile -> ring slot i % kDRing; rows
+        // past the item's end belong to the next item and only feed visibilities never stored
+        if (lane == 0) {
+            int issued = 0;
+            for (int i = 0; i < ntiles; i++) {
+                const int slot = i % kDRing;
+                const uint32_t ph = (i / kDRing) & 1;
+                if (!mbar_wait(&in_empty[slot], ph ^ 1, abort_flag, kWaitNs)) {
+                    *abort_flag = 1;
+                    atomicOr(a.status, kStatusWait);
+                    break;
+                }
+                mbar_expect_tx(&in_full[slot], kDTile * 16);
+                tma_load_2d(rbase + slot * kDRingSlot, &maps.coef, 0, static_cast<int32_t>(c0 + i * kDTile),
+                            &in_full[slot]);
+                issued = i + 1;
+            }
+            volatile int never = 0;
+            for (int i = issued > kDRing ? issued - kDRing : 0; i < issued; i++)
+                if (!mbar_wait(&in_full[i % kDRing], (i / kDRing) & 1, &never, kWaitNs)) atomicOr(a.status, kStatusWait);
         }
         __syncwarp();
     } else if (warp == kDLoaderWarp) {
@@ -868,24 +934,52 @@ static p9idg_status launch_coef(TcPlanState &st, const GridderArgs &a, int32_t n
     return P9IDG_OK;
 }
 
+namespace {
+
+template <bool BF16, typename VisT, bool BATCH, bool TMA>
+cudaError_t run_gridder(const TcArgs &t, const TcArgs *probs, int32_t nitems, const TmaMaps &maps,
+                        cudaStream_t stream) {
+    cudaError_t e = set_smem(tc_gridder_kernel<BF16, VisT, BATCH, TMA>, kGSmem);
+    if (e == cudaSuccess) tc_gridder_kernel<BF16, VisT, BATCH, TMA><<<nitems, kGThreads, kGSmem, stream>>>(t, probs, maps);
+    return e;
+}
+
+template <bool BF16, typename OutT, bool BATCH, bool TMA>
+cudaError_t run_degridder(const TcArgs &t, const TcArgs *probs, int32_t nitems, const TmaMaps &maps,
+                          cudaStream_t stream) {
+    cudaError_t e = set_smem(tc_degridder_kernel<BF16, OutT, BATCH, TMA>, kDSmem);
+    if (e == cudaSuccess)
+        tc_degridder_kernel<BF16, OutT, BATCH, TMA><<<nitems, kDThreads, kDSmem, stream>>>(t, probs, maps);
+    return e;
+}
+
+// maps: TMA staging for a single-plan launch (nullptr: cp.async staging).  Batched launches read
+// per-problem buffers and always use cp.async.
 template <bool BATCH>
-static p9idg_status launch_tc_gridder(const TcArgs &t, const TcArgs *probs, int32_t nitems, bool c128, int mode,
-                                      cudaStream_t stream, std::string &err) {
+p9idg_status launch_tc_gridder(const TcArgs &t, const TcArgs *probs, int32_t nitems, bool c128, int mode,
+                               const TmaMaps *maps, cudaStream_t stream, std::string &err) {
     if (nitems == 0) return P9IDG_OK;
+    static const TmaMaps kNoMaps{};
     const bool bf16 = mode == P9IDG_MODE_TC_BF16X3;
-    cudaError_t e;
-    if (bf16 && c128) {
-        e = set_smem(tc_gridder_kernel<true, double2, BATCH>, kGSmem);
-        if (e == cudaSuccess) tc_gridder_kernel<true, double2, BATCH><<<nitems, kGThreads, kGSmem, stream>>>(t, probs);
-    } else if (bf16) {
-        e = set_smem(tc_gridder_kernel<true, float2, BATCH>, kGSmem);
-        if (e == cudaSuccess) tc_gridder_kernel<true, float2, BATCH><<<nitems, kGThreads, kGSmem, stream>>>(t, probs);
-    } else if (c128) {
-        e = set_smem(tc_gridder_kernel<false, double2, BATCH>, kGSmem);
-        if (e == cudaSuccess) tc_gridder_kernel<false, double2, BATCH><<<nitems, kGThreads, kGSmem, stream>>>(t, probs);
-    } else {
-        e = set_smem(tc_gridder_kernel<false, float2, BATCH>, kGSmem);
-        if (e == cudaSuccess) tc_gridder_kernel<false, float2, BATCH><<<nitems, kGThreads, kGSmem, stream>>>(t, probs);
+    const TmaMaps &m = maps ? *maps : kNoMaps;
+    cudaError_t e = cudaSuccess;
+    bool done = false;
+    if constexpr (!BATCH) {
+        if (maps && !c128) {
+            e = bf16 ? run_gridder<true, float2, false, true>(t, probs, nitems, m, stream)
+                     : run_gridder<false, float2, false, true>(t, probs, nitems, m, stream);
+            done = true;
+        }
+    }
+    if (!done) {
+        if (bf16 && c128)
+            e = run_gridder<true, double2, BATCH, false>(t, probs, nitems, m, stream);
+        else if (bf16)
+            e = run_gridder<true, float2, BATCH, false>(t, probs, nitems, m, stream);
+        else if (c128)
+            e = run_gridder<false, double2, BATCH, false>(t, probs, nitems, m, stream);
+        else
+            e = run_gridder<false, float2, BATCH, false>(t, probs, nitems, m, stream);
     }
     if (e == cudaSuccess) e = cudaGetLastError();
     if (e != cudaSuccess) {
@@ -896,23 +990,36 @@ static p9idg_status launch_tc_gridder(const TcArgs &t, const TcArgs *probs, int3
 }
 
 template <bool BATCH>
-static p9idg_status launch_tc_degridder(const TcArgs &t, const TcArgs *probs, int32_t nitems, bool c128, int mode,
-                                        cudaStream_t stream, std::string &err) {
+p9idg_status launch_tc_degridder(const TcArgs &t, const TcArgs *probs, int32_t nitems, bool c128, int mode,
+                                 const TmaMaps *maps, cudaStream_t stream, std::string &err) {
     if (nitems == 0) return P9IDG_OK;
+    static const TmaMaps kNoMaps{};
     const bool bf16 = mode == P9IDG_MODE_TC_BF16X3;
-    cudaError_t e;
-    if (bf16 && c128) {
-        e = set_smem(tc_degridder_kernel<true, double2, BATCH>, kDSmem);
-        if (e == cudaSuccess) tc_degridder_kernel<true, double2, BATCH><<<nitems, kDThreads, kDSmem, stream>>>(t, probs);
-    } else if (bf16) {
-        e = set_smem(tc_degridder_kernel<true, float2, BATCH>, kDSmem);
-        if (e == cudaSuccess) tc_degridder_kernel<true, float2, BATCH><<<nitems, kDThreads, kDSmem, stream>>>(t, probs);
-    } else if (c128) {
-        e = set_smem(tc_degridder_kernel<false, double2, BATCH>, kDSmem);
-        if (e == cudaSuccess) tc_degridder_kernel<false, double2, BATCH><<<nitems, kDThreads, kDSmem, stream>>>(t, probs);
-    } else {
-        e = set_smem(tc_degridder_kernel<false, float2, BATCH>, kDSmem);
-        if (e == cudaSuccess) tc_degridder_kernel<false, float2, BATCH><<<nitems, kDThreads, kDSmem, stream>>>(t, probs);
+    const TmaMaps &m = maps ? *maps : kNoMaps;
+    cudaError_t e = cudaSuccess;
+    bool done = false;
+    if constexpr (!BATCH) {
+        if (maps) {
+            if (bf16 && c128)
+                e = run_degridder<true, double2, false, true>(t, probs, nitems, m, stream);
+            else if (bf16)
+                e = run_degridder<true, float2, false, true>(t, probs, nitems, m, stream);
+            else if (c128)
+                e = run_degridder<false, double2, false, true>(t, probs, nitems, m, stream);
+            else
+                e = run_degridder<false, float2, false, true>(t, probs, nitems, m, stream);
+            done = true;
+        }
+    }
+    if (!done) {
+        if (bf16 && c128)
+            e = run_degridder<true, double2, BATCH, false>(t, probs, nitems, m, stream);
+        else if (bf16)
+            e = run_degridder<true, float2, BATCH, false>(t, probs, nitems, m, stream);
+        else if (c128)
+            e = run_degridder<false, double2, BATCH, false>(t, probs, nitems, m, stream);
+        else
+            e = run_degridder<false, float2, BATCH, false>(t, probs, nitems, m, stream);
     }
     if (e == cudaSuccess) e = cudaGetLastError();
     if (e != cudaSuccess) {
@@ -921,6 +1028,53 @@ static p9idg_status launch_tc_degridder(const TcArgs &t, const TcArgs *probs, in
     }
     return P9IDG_OK;
 }
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link to the driver library).
+using EncodeTiledFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                   const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_tiled() {
+    static const EncodeTiledFn fn = [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            return static_cast<EncodeTiledFn>(nullptr);
+        return reinterpret_cast<EncodeTiledFn>(p);
+    }();
+    return fn;
+}
+
+// Tensor maps over the coefficients (tiles of box_rows float4 rows) and, when vis is given,
+// over nvis complex64 visibilities; false (use cp.async) when a map cannot be made.
+bool make_maps(TmaMaps &m, const float4 *coef, int64_t ncoef, int box_rows, const void *vis, int64_t nvis) {
+    const EncodeTiledFn fn = encode_tiled();
+    constexpr int64_t kMaxCoord = (int64_t(1) << 31) - 1024;  // TMA coordinates are signed 32-bit
+    if (!fn || !coef || ncoef <= 0 || ncoef > kMaxCoord || (reinterpret_cast<uintptr_t>(coef) & 15)) return false;
+    const cuuint64_t cdim[2] = {4, static_cast<cuuint64_t>(ncoef)};
+    const cuuint64_t cstride[1] = {16};
+    const cuuint32_t cbox[2] = {4, static_cast<cuuint32_t>(box_rows)};
+    const cuuint32_t ones[2] = {1, 1};
+    if (fn(&m.coef, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float4 *>(coef), cdim, cstride, cbox, ones,
+           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return false;
+    if (vis) {
+        if (nvis <= 0 || nvis > kMaxCoord || (reinterpret_cast<uintptr_t>(vis) & 15)) return false;
+        const cuuint64_t vdim[1] = {static_cast<cuuint64_t>(nvis)};
+        const cuuint64_t vstride[1] = {8};
+        const cuuint32_t vbox[1] = {kVisBox};
+        if (fn(&m.vis, CU_TENSOR_MAP_DATA_TYPE_UINT64, 1, const_cast<void *>(vis), vdim, vstride, vbox, ones,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+            return false;
+    }
+    return true;
+}
+
+}  // namespace
 
 void tc_fill_args(const TcPlanState &st, const GridderArgs &a, TcArgs &t) {
     fill_args(t, a, st);
@@ -947,7 +1101,11 @@ p9idg_status tc_grid(TcPlanState &st, const GridderArgs &a, int mode, cudaStream
     if (s != P9IDG_OK) return s;
     TcArgs t{};
     tc_fill_args(st, a, t);
-    return launch_tc_gridder<false>(t, nullptr, a.nitems, a.vis_c128, mode, stream, err);
+    TmaMaps maps;
+    const int64_t nvis = static_cast<int64_t>(a.g.nbl) * a.g.nt_all * a.g.nch;
+    const bool tma =
+        !a.vis_c128 && make_maps(maps, static_cast<const float4 *>(st.coef), st.ncoef, kGVps, a.vis, nvis);
+    return launch_tc_gridder<false>(t, nullptr, a.nitems, a.vis_c128, mode, tma ? &maps : nullptr, stream, err);
 }
 
 p9idg_status tc_degrid(TcPlanState &st, const GridderArgs &a, int mode, cudaStream_t stream, std::string &err) {
@@ -956,21 +1114,23 @@ p9idg_status tc_degrid(TcPlanState &st, const GridderArgs &a, int mode, cudaStre
     TcArgs t{};
     tc_fill_args(st, a, t);
     t.items = static_cast<const WorkItem *>(st.ditems);
-    return launch_tc_degridder<false>(t, nullptr, st.nditems, a.out_c128, mode, stream, err);
+    TmaMaps maps;
+    const bool tma = make_maps(maps, static_cast<const float4 *>(st.coef), st.ncoef, kDTile, nullptr, 0);
+    return launch_tc_degridder<false>(t, nullptr, st.nditems, a.out_c128, mode, tma ? &maps : nullptr, stream, err);
 }
 
 p9idg_status tc_grid_batch(const TcArgs *probs, const WorkItem *items, int32_t nitems, int mode,
                            cudaStream_t stream, std::string &err) {
     TcArgs t{};
     t.items = items;
-    return launch_tc_gridder<true>(t, probs, nitems, false, mode, stream, err);
+    return launch_tc_gridder<true>(t, probs, nitems, false, mode, nullptr, stream, err);
 }
 
 p9idg_status tc_degrid_batch(const TcArgs *probs, const WorkItem *items, int32_t nitems, int mode,
                              cudaStream_t stream, std::string &err) {
     TcArgs t{};
     t.items = items;
-    return launch_tc_degridder<true>(t, probs, nitems, false, mode, stream, err);
+    return launch_tc_degridder<true>(t, probs, nitems, false, mode, nullptr, stream, err);
 }
 
 void tc_release(TcPlanState &st) {
