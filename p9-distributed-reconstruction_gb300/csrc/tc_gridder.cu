@@ -56,6 +56,14 @@ struct TmaMaps {
 };
 constexpr int kVisBox = 34;
 
+// The dynamic shared memory rounded up to a 1 KB boundary by pointer arithmetic on the
+// __shared__ array itself, so that every pointer derived from it stays in the shared state
+// space and its loads and stores compile to shared-memory instructions (an integer round trip
+// would leave generic pointers behind).
+__device__ __forceinline__ unsigned char *smem_1k(unsigned char *raw) {
+    return raw + ((1024u - (smem_u32(raw) & 1023u)) & 1023u);
+}
+
 // ---------------- bf16 / fp16 splitting ----------------
 
 template <bool BF16>
@@ -178,7 +186,7 @@ template <bool BF16, typename VisT, bool BATCH, bool TMA>
 __global__ void __launch_bounds__(kGThreads, 3)
     tc_gridder_kernel(const TcArgs L, const TcArgs *__restrict__ probs, const __grid_constant__ TmaMaps maps) {
     extern __shared__ unsigned char smem_raw[];
-    unsigned char *smem = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    unsigned char *smem = smem_1k(smem_raw);
     unsigned char *ring = smem + kGStages * kGStageBytes;
     uint64_t *full = reinterpret_cast<uint64_t *>(ring + kGRing * kGRingSlot);
     uint64_t *empty = full + kGStages;
@@ -343,12 +351,17 @@ __global__ void __launch_bounds__(kGThreads, 3)
                 for (int v = 0; v < 4; v++) {
                     c[v] = rc[v];
                     vv[v] = load_vis(rv, v);
-                    // a TMA tile past the item's end holds the next item's samples: weight them 0
-                    if (TMA && i * kGVps + group * 4 + v >= nvis) vv[v] = make_float2(0.f, 0.f);
+                }
+                // a TMA tile past the item's end holds the next item's samples: weight them 0
+                if (TMA && i == nstages - 1) {
+#pragma unroll
+                    for (int v = 0; v < 4; v++)
+                        if (i * kGVps + group * 4 + v >= nvis) vv[v] = make_float2(0.f, 0.f);
                 }
             }
-            __syncwarp();
-            if (lane == 0) mbar_arrive(&in_empty[slot]);
+            // the ring slot is released only after the values read from it have been used (below):
+            // an arrive right after the loads could let the next copy into the slot overtake a
+            // shared-memory load still queued, which would then return the next stage's data
             if (!warp_wait(&empty[s], ph ^ 1, abort_flag, kWaitNs)) {
                 if (lane == 0) {
                     *abort_flag = 1;
@@ -389,7 +402,10 @@ __global__ void __launch_bounds__(kGThreads, 3)
             st_shared_v4(B + chunk_off(32 + lane, group), bhi[0], bhi[1], bhi[2], bhi[3]);
             fence_proxy_async();
             __syncwarp();
-            if (lane == 0) mbar_arrive(&full[s]);
+            if (lane == 0) {
+                mbar_arrive(&full[s]);
+                mbar_arrive(&in_empty[slot]);
+            }
         }
         // ---- epilogue: TMEM -> smem planes -> partial subgrid
         const bool ok = warp_wait(accb, 0, abort_flag, kWaitNs);
@@ -400,7 +416,7 @@ __global__ void __launch_bounds__(kGThreads, 3)
         if (ok && plane >= 0) {
             uint32_t r[32];
             tmem_ld32(tmem + (static_cast<uint32_t>(32 * q) << 16) + static_cast<uint32_t>(half * 32), r);
-            tmem_ld_wait();
+            tmem_ld_wait(r);
 #pragma unroll
             for (int j = 0; j < 32; j++) E[plane * 32 * 33 + lane * 33 + j] = __uint_as_float(r[j]);
         }
@@ -453,7 +469,7 @@ template <bool BF16, typename OutT, bool BATCH, bool TMA>
 __global__ void __launch_bounds__(kDThreads, 2)
     tc_degridder_kernel(const TcArgs L, const TcArgs *__restrict__ probs, const __grid_constant__ TmaMaps maps) {
     extern __shared__ unsigned char smem_raw[];
-    unsigned char *smem = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    unsigned char *smem = smem_1k(smem_raw);
     unsigned char *bstat = smem;
     unsigned char *tiles = smem + kDStatic;
     unsigned char *ring = tiles + 2 * kDTileBytes;
@@ -656,8 +672,7 @@ __global__ void __launch_bounds__(kDThreads, 2)
                     cu[u] = make_float2(c.x, c.z);
                 }
             }
-            __syncwarp();
-            if (lane == 0) mbar_arrive(&in_empty[slot]);
+            // the slot is released once cu has been used (below), not right after the loads
             if (!warp_wait(&a_empty[b], ph ^ 1, abort_flag, kWaitNs)) {
                 if (lane == 0) {
                     *abort_flag = 1;
@@ -681,7 +696,10 @@ __global__ void __launch_bounds__(kDThreads, 2)
             }
             fence_proxy_async();
             __syncwarp();
-            if (lane == 0) mbar_arrive(&a_full[b]);
+            if (lane == 0) {
+                mbar_arrive(&a_full[b]);
+                mbar_arrive(&in_empty[slot]);
+            }
         }
     } else {
         // ---- epilogue: one visibility per thread
@@ -699,8 +717,7 @@ __global__ void __launch_bounds__(kDThreads, 2)
                 break;
             }
             const float4 c = reinterpret_cast<const float4 *>(ring + slot * kDRingSlot)[row];
-            __syncwarp();
-            if (lane == 0) mbar_arrive(&in_empty[slot]);
+            // the slot is released once c has been used (below), not right after the load
             if (!warp_wait(&acc_full[b], ph, abort_flag, kWaitNs)) {
                 if (lane == 0) {
                     *abort_flag = 1;
@@ -717,7 +734,8 @@ __global__ void __launch_bounds__(kDThreads, 2)
                 uint32_t t0[32], t1[32];
                 tmem_ld32(acc + h * 32, t0);
                 tmem_ld32(acc + 64 + h * 32, t1);
-                tmem_ld_wait();
+                tmem_ld_wait(t0);
+                tmem_ld_wait(t1);
 #pragma unroll
                 for (int yy = 0; yy < 16; yy++) {
                     const int y = h * 16 + yy;
@@ -732,7 +750,10 @@ __global__ void __launch_bounds__(kDThreads, 2)
             }
             tc_fence_before();
             __syncwarp();
-            if (lane == 0) mbar_arrive(&acc_empty[b]);
+            if (lane == 0) {
+                mbar_arrive(&acc_empty[b]);
+                mbar_arrive(&in_empty[slot]);
+            }
             if (j < nvis) {
                 const float sc = g.inv_s2 / sq;  // exact: sq is a power of two
                 store_vis(out, j, make_float2(vre * sc, vim * sc));
@@ -761,7 +782,7 @@ template <bool BF16>
 __global__ void __launch_bounds__(128) tc_selftest_kernel(const float *A, const float *B, int N, float *C,
                                                           int32_t *status) {
     extern __shared__ unsigned char smem_raw[];
-    unsigned char *smem = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    unsigned char *smem = smem_1k(smem_raw);
     unsigned char *sa = smem, *sb = smem + 128 * 128;
     uint64_t *bar = reinterpret_cast<uint64_t *>(sb + 128 * 128);
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bar + 1);
@@ -809,7 +830,7 @@ __global__ void __launch_bounds__(128) tc_selftest_kernel(const float *A, const 
         for (int c0 = 0; c0 < N; c0 += 32) {
             uint32_t r[32];
             tmem_ld32(tmem + (static_cast<uint32_t>(32 * warp) << 16) + c0, r);
-            tmem_ld_wait();
+            tmem_ld_wait(r);
             for (int j = 0; j < 32; j++) C[(32 * warp + lane) * N + c0 + j] = __uint_as_float(r[j]);
         }
     }

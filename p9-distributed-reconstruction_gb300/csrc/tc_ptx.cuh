@@ -106,15 +106,19 @@ __device__ __forceinline__ void fence_proxy_async() {
 }
 
 // ---- tcgen05: TMEM ----
+// alloc, relinquish and dealloc are .sync.aligned as well: the warp is reconverged first
 __device__ __forceinline__ void tmem_alloc(uint32_t *dst_smem, uint32_t ncols) {  // whole warp
+    __syncwarp();
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(dst_smem)),
                  "r"(ncols)
                  : "memory");
 }
 __device__ __forceinline__ void tmem_relinquish() {  // whole warp
+    __syncwarp();
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
 }
 __device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {  // whole warp
+    __syncwarp();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
 }
 __device__ __forceinline__ void tc_fence_before() {
@@ -158,7 +162,12 @@ __device__ __forceinline__ void mma_commit(uint64_t *bar) {
 }
 
 // ---- tcgen05: TMEM -> registers (32 lanes x 32 columns of 32 bits per warp) ----
+// tcgen05.ld and tcgen05.wait::ld are .sync.aligned: all 32 lanes must execute the same
+// instruction together.  Callers reach them after lane-0-only mbarrier polling, and nothing
+// obliges the compiler to reconverge the warp there, so both helpers reconverge it first.
+// Every lane of the warp must call them.
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+    __syncwarp();
     asm volatile(
         "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
         "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
@@ -170,7 +179,20 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
         : "r"(taddr)
         : "memory");
 }
-__device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+// Waits for this thread's outstanding tcgen05.ld and hands r back as its output: the loaded
+// registers carry no dependence on a bare wait, so without the operands the compiler could
+// schedule arithmetic on them before the data has arrived.  With two loads in flight, call it
+// once per destination array (the second wait finds nothing outstanding).
+__device__ __forceinline__ void tmem_ld_wait(uint32_t (&r)[32]) {
+    __syncwarp();
+    asm volatile("tcgen05.wait::ld.sync.aligned;"
+                 : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]),
+                   "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]), "+r"(r[15]),
+                   "+r"(r[16]), "+r"(r[17]), "+r"(r[18]), "+r"(r[19]), "+r"(r[20]), "+r"(r[21]), "+r"(r[22]), "+r"(r[23]),
+                   "+r"(r[24]), "+r"(r[25]), "+r"(r[26]), "+r"(r[27]), "+r"(r[28]), "+r"(r[29]), "+r"(r[30]), "+r"(r[31])
+                 :
+                 : "memory");
+}
 
 }  // namespace tc
 }  // namespace p9idg
