@@ -145,7 +145,16 @@ struct p9idg_plan {
     bool gaps_ready = false;
     DevBuf d_gaps;
     cudaStream_t side = nullptr;  // the D2H copy of DeGrid's shifted grid runs here, beside the degridder
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_mid = nullptr;
+    // In-place GridW: the gridder items and the subgrids regrouped so that every w layer but the
+    // busiest one is gridded and added first; those layers then cross the link while the busiest
+    // one grids.  Items keep their partial-subgrid slots; built with the gridder items.
+    std::vector<WorkItem> gitems_lyr;  // items of the other layers, then of the busiest layer
+    std::vector<int32_t> sub_lyr;      // subgrid indices in the same grouping
+    int32_t lyr_minor_items = 0, lyr_minor_subs = 0, lyr_major = -1;
+    bool lyr_ready = false;
+    DevBuf d_gitems_lyr, d_sub_lyr, d_zero128;
+    DevBuf d_uvw_prev, d_uvw_flag;  // the previous uvw upload and the "uvw differs" flag
 
     bool timing = false;
     std::vector<PendingTiming> pending;
@@ -236,6 +245,7 @@ void build_gridder_items(p9idg_plan *p) {
     p->nslots = 0;
     for (const auto &d : p->dsub) p->nslots += d.item_count;
     p->items_dirty = true;
+    p->lyr_ready = false;
 }
 
 void finish_plan(p9idg_plan *p) {
@@ -276,6 +286,7 @@ p9idg_status ensure_device(p9idg_plan *p) {
     CK(cudaStreamCreateWithFlags(&p->side, cudaStreamNonBlocking));
     CK(cudaEventCreateWithFlags(&p->ev_fork, cudaEventDisableTiming));
     CK(cudaEventCreateWithFlags(&p->ev_join, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&p->ev_mid, cudaEventDisableTiming));
     {
         int pageable = 0, host_tables = 0;
         CK(cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, p->device));
@@ -305,7 +316,21 @@ p9idg_status upload_uvw(p9idg_plan *p, const double *uvw) {
     CK(p->d_uvw.ensure(bytes));
     if (uvw) {
         StageScope t(p, P9IDG_STAGE_H2D);
-        CK(cudaMemcpyAsync(p->d_uvw.p, uvw, bytes, cudaMemcpyHostToDevice, p->stream));
+        if (p->tc.coef_valid) {
+            // the tensor-core coefficients exist for the uvw now in d_uvw: the new upload goes to
+            // the other buffer and is compared with it on the device, and the coefficient kernel
+            // recomputes only if some word differs (no host synchronisation either way)
+            std::swap(p->d_uvw, p->d_uvw_prev);
+            CK(p->d_uvw.ensure(bytes));
+            CK(p->d_uvw_flag.ensure(sizeof(int32_t)));
+            CK(cudaMemcpyAsync(p->d_uvw.p, uvw, bytes, cudaMemcpyHostToDevice, p->stream));
+            CK(launch_words_differ(p->d_uvw.p, p->d_uvw_prev.p, static_cast<int64_t>(bytes / 8),
+                                   p->d_uvw_flag.as<int32_t>(), p->stream));
+            p->tc.coef_recompute_flag = p->d_uvw_flag.as<int32_t>();
+        } else {
+            CK(cudaMemcpyAsync(p->d_uvw.p, uvw, bytes, cudaMemcpyHostToDevice, p->stream));
+            p->tc.coef_recompute_flag = nullptr;
+        }
         p->uvw_uploaded = (uvw == p->uvw.data());
         p->tc.coef_valid = false;
     } else if (!p->uvw_uploaded) {
@@ -313,6 +338,7 @@ p9idg_status upload_uvw(p9idg_plan *p, const double *uvw) {
         CK(cudaMemcpyAsync(p->d_uvw.p, p->uvw.data(), bytes, cudaMemcpyHostToDevice, p->stream));
         p->uvw_uploaded = true;
         p->tc.coef_valid = false;
+        p->tc.coef_recompute_flag = nullptr;
     }
     return P9IDG_OK;
 }
@@ -335,7 +361,9 @@ p9idg_status upload_items(p9idg_plan *p) {
     return P9IDG_OK;
 }
 
-p9idg_status prepare(p9idg_plan *p, const double *uvw) {
+// Device state for a call, without the uvw upload (in-place host calls start their transfers in
+// the other direction first and upload uvw beside them).
+p9idg_status prepare_state(p9idg_plan *p) {
     TRY(ensure_device(p));
     if (p->items_dirty) TRY(upload_items(p));
     if (p->taper_dirty) {
@@ -344,6 +372,11 @@ p9idg_status prepare(p9idg_plan *p, const double *uvw) {
         p->taper_dirty = false;
     }
     CK(cudaMemsetAsync(p->d_status.p, 0, sizeof(int32_t), p->stream));
+    return P9IDG_OK;
+}
+
+p9idg_status prepare(p9idg_plan *p, const double *uvw) {
+    TRY(prepare_state(p));
     return upload_uvw(p, uvw);
 }
 
@@ -415,36 +448,56 @@ p9idg_status check_wstack_layers(const p9idg_plan *p) {
 }
 
 // vis (device, complex64 or complex128) -> layers (device complex64, W or 1 grids)
-p9idg_status run_grid(p9idg_plan *p, const void *d_vis, bool vis_c128, float2 *d_layers, bool wstack) {
-    const int N = p->c.grid_size, S = p->c.subgrid_size;
-    const int nl = wstack ? p->c.wlayer_count : 1;
+size_t vis_count_of(const p9idg_plan *p) { return static_cast<size_t>(p->nbl) * p->nt * p->nch; }
+size_t nn_of(const p9idg_plan *p) { return static_cast<size_t>(p->c.grid_size) * p->c.grid_size; }
+
+// Gridder over nitems work items (all of the plan's, or a group of them) into their partial slots.
+p9idg_status grid_items(p9idg_plan *p, const void *d_vis, bool vis_c128, const WorkItem *d_items, int32_t nitems) {
+    const int S = p->c.subgrid_size;
     CK(p->d_partials.ensure(sizeof(float2) * S * S * std::max<size_t>(1, p->nslots)));
-    {
-        StageScope t(p, P9IDG_STAGE_GRIDDER);
-        GridderArgs a = gridder_args(p);
-        a.items = p->d_gitems.as<WorkItem>();
-        a.nitems = static_cast<int32_t>(p->gitems.size());
-        a.vis = d_vis;
-        a.vis_c128 = vis_c128;
-        a.partials = p->d_partials.as<float2>();
-        if (use_tc(p)) {
-            TRY(ensure_tc(p));
-            TRY(tc_grid(p->tc, a, p->mode, p->stream, g_last_error));
-        } else {
-            CK(launch_gridder_fp32(a, p->stream));
-        }
-    }
-    {
-        StageScope t(p, P9IDG_STAGE_SUBGRID_IFFT_ADD);
-        CK(cudaMemsetAsync(d_layers, 0, sizeof(float2) * static_cast<size_t>(nl) * N * N, p->stream));
-        SubgridOpArgs a = subgrid_args(p);
-        a.partials = p->d_partials.as<float2>();
-        a.layers = d_layers;
-        a.out_shifted = true;  // IDG.cs:17,37
-        a.wstack = wstack;
-        CK(launch_subgrid_ifft_add(a, p->stream));
+    StageScope t(p, P9IDG_STAGE_GRIDDER);
+    GridderArgs a = gridder_args(p);
+    a.items = d_items;
+    a.nitems = nitems;
+    a.vis = d_vis;
+    a.vis_c128 = vis_c128;
+    a.partials = p->d_partials.as<float2>();
+    if (use_tc(p)) {
+        TRY(ensure_tc(p));
+        TRY(tc_grid(p->tc, a, p->mode, p->stream, g_last_error));
+    } else {
+        CK(launch_gridder_fp32(a, p->stream));
     }
     return P9IDG_OK;
+}
+
+// Subgrid IFFT + adder of nsub subgrids (all, or the subgrid list d_list) into the layers.
+p9idg_status add_subgrids(p9idg_plan *p, float2 *d_layers, bool wstack, const int32_t *d_list, int32_t nsub) {
+    StageScope t(p, P9IDG_STAGE_SUBGRID_IFFT_ADD);
+    SubgridOpArgs a = subgrid_args(p);
+    a.partials = p->d_partials.as<float2>();
+    a.layers = d_layers;
+    a.out_shifted = true;  // IDG.cs:17,37
+    a.wstack = wstack;
+    if (d_list) {
+        a.sub_list = d_list;
+        a.nsub = nsub;
+    }
+    CK(launch_subgrid_ifft_add(a, p->stream));
+    return P9IDG_OK;
+}
+
+p9idg_status clear_layers(p9idg_plan *p, float2 *d_layers, int nl) {
+    StageScope t(p, P9IDG_STAGE_SUBGRID_IFFT_ADD);
+    CK(cudaMemsetAsync(d_layers, 0, sizeof(float2) * static_cast<size_t>(nl) * nn_of(p), p->stream));
+    return P9IDG_OK;
+}
+
+p9idg_status run_grid(p9idg_plan *p, const void *d_vis, bool vis_c128, float2 *d_layers, bool wstack) {
+    const int nl = wstack ? p->c.wlayer_count : 1;
+    TRY(grid_items(p, d_vis, vis_c128, p->d_gitems.as<WorkItem>(), static_cast<int32_t>(p->gitems.size())));
+    TRY(clear_layers(p, d_layers, nl));
+    return add_subgrids(p, d_layers, wstack, nullptr, 0);
 }
 
 // grid (device complex64) -> vis (device, complex64 or complex128); uncovered samples are 0
@@ -490,9 +543,6 @@ p9idg_status run_degrid(p9idg_plan *p, const float2 *d_grid, bool grid_shifted, 
     }
     return P9IDG_OK;
 }
-
-size_t vis_count_of(const p9idg_plan *p) { return static_cast<size_t>(p->nbl) * p->nt * p->nch; }
-size_t nn_of(const p9idg_plan *p) { return static_cast<size_t>(p->c.grid_size) * p->c.grid_size; }
 
 p9idg_status h2d(p9idg_plan *p, void *dst, const void *src, size_t bytes) {
     StageScope t(p, P9IDG_STAGE_H2D);
@@ -565,40 +615,175 @@ p9idg_status ensure_gaps(p9idg_plan *p) {
 
 bool host_in_place(const p9idg_plan *p) { return p->host_direct && p->host_access != 0; }
 
+// Target w layer of each subgrid as AdderWStack.Add places it (AdderWStack.cs:38-51; -1: skipped),
+// the busiest layer by gridded time samples, and the gridder items and subgrids regrouped as
+// [every other layer | the busiest layer].  With no work outside the busiest layer there is
+// nothing to overlap and lyr_minor_items stays 0.
+p9idg_status ensure_layer_split(p9idg_plan *p) {
+    if (p->lyr_ready) return P9IDG_OK;
+    const int N = p->c.grid_size, S = p->c.subgrid_size, W = p->c.wlayer_count;
+    std::vector<int32_t> layer(p->subs.size(), -1);
+    std::vector<int64_t> work(std::max(W, 1), 0);
+    for (size_t i = 0; i < p->subs.size(); i++) {
+        const auto &sg = p->subs[i];
+        int sx = sg.u_pixel, sy = sg.v_pixel, sw = sg.w_lambda;
+        if (sw < 0) {
+            sx = N - sx - S + 1;
+            sy = N - sy - S + 1;
+            sw = -sw - 1;
+        }
+        if (sx >= 1 && sx < N - S && sy >= 1 && sy < N - S && sw >= 0 && sw < W) {
+            layer[i] = sw;
+            work[sw] += sg.time_sample_count;
+        }
+    }
+    p->lyr_major = -1;
+    int64_t best = 0, total = 0;
+    for (int k = 0; k < W; k++) {
+        total += work[k];
+        if (work[k] > best) {
+            best = work[k];
+            p->lyr_major = k;
+        }
+    }
+    p->gitems_lyr.clear();
+    p->sub_lyr.clear();
+    p->lyr_minor_items = p->lyr_minor_subs = 0;
+    if (p->lyr_major >= 0 && total > best) {
+        const int32_t major = p->lyr_major;
+        for (int pass = 0; pass < 2; pass++) {
+            const bool want_major = pass == 1;
+            for (const auto &it : p->gitems)
+                if ((layer[it.subgrid] == major) == want_major) p->gitems_lyr.push_back(it);
+            for (size_t i = 0; i < layer.size(); i++)
+                if ((layer[i] == major) == want_major) p->sub_lyr.push_back(static_cast<int32_t>(i));
+            if (pass == 0) {
+                p->lyr_minor_items = static_cast<int32_t>(p->gitems_lyr.size());
+                p->lyr_minor_subs = static_cast<int32_t>(p->sub_lyr.size());
+            }
+        }
+        CK(p->d_gitems_lyr.ensure(sizeof(WorkItem) * p->gitems_lyr.size()));
+        CK(p->d_sub_lyr.ensure(sizeof(int32_t) * p->sub_lyr.size()));
+        CK(cudaMemcpyAsync(p->d_gitems_lyr.p, p->gitems_lyr.data(), sizeof(WorkItem) * p->gitems_lyr.size(),
+                           cudaMemcpyHostToDevice, p->stream));
+        CK(cudaMemcpyAsync(p->d_sub_lyr.p, p->sub_lyr.data(), sizeof(int32_t) * p->sub_lyr.size(),
+                           cudaMemcpyHostToDevice, p->stream));
+        CK(cudaStreamSynchronize(p->stream));
+    }
+    p->lyr_ready = true;
+    return P9IDG_OK;
+}
+
+// Page-locked host memory (first and last byte): written by the copy engines, which reach the
+// link's full device-to-host rate; pageable memory reached through the host page tables is
+// written by kernels instead.
+bool host_pinned(const void *ptr, size_t bytes) {
+    for (const char *q : {static_cast<const char *>(ptr), static_cast<const char *>(ptr) + bytes - 1}) {
+        cudaPointerAttributes at{};
+        if (cudaPointerGetAttributes(&at, q) != cudaSuccess) {
+            (void)cudaGetLastError();
+            return false;
+        }
+        if (at.type != cudaMemoryTypeHost) return false;
+    }
+    return true;
+}
+
+// One complex64 layer -> the caller's complex128 layer in host memory: widened on the device into
+// the staging slot and copied by a copy engine (pinned), or widened straight into host memory.
+p9idg_status layer_to_host(const float2 *d_layer, size_t nn, double2 *h_out, double2 *d_stage, bool pinned,
+                           cudaStream_t st) {
+    if (pinned) {
+        CK(launch_c64_to_c128(d_layer, static_cast<int64_t>(nn), d_stage, st));
+        CK(cudaMemcpyAsync(h_out, d_stage, sizeof(double2) * nn, cudaMemcpyDeviceToHost, st));
+    } else {
+        CK(launch_c64_to_c128(d_layer, static_cast<int64_t>(nn), h_out, st));
+    }
+    return P9IDG_OK;
+}
+
+// Zeros one complex128 layer of the caller's output in host memory.
+p9idg_status zero_host_layer(p9idg_plan *p, double2 *h_out, size_t nn, bool pinned, cudaStream_t st) {
+    if (pinned) {
+        if (p->d_zero128.bytes < sizeof(double2) * nn) {
+            CK(p->d_zero128.ensure(sizeof(double2) * nn));
+            CK(cudaMemsetAsync(p->d_zero128.p, 0, sizeof(double2) * nn, st));
+        }
+        CK(cudaMemcpyAsync(h_out, p->d_zero128.p, sizeof(double2) * nn, cudaMemcpyDeviceToHost, st));
+    } else {
+        CK(launch_zero_c128(h_out, static_cast<int64_t>(nn), st));
+    }
+    return P9IDG_OK;
+}
+
+
 p9idg_status host_grid_common(p9idg_plan *p, const double *vis, const double *uvw, double *out, bool wstack) {
     if (!p || !vis || !out) return fail(P9IDG_INVALID_ARGUMENT, "null argument");
     TRY(wstack ? check_wstack_layers(p) : check_adder_range(p));
-    TRY(prepare(p, uvw));
+    TRY(prepare_state(p));
     const size_t nvis = vis_count_of(p), nl = wstack ? p->c.wlayer_count : 1;
     if (host_in_place(p)) {
-        // The gridder reads the caller's complex128 visibilities in host memory, once each, and the
-        // widening of the layers writes straight into the caller's output.  Layers no subgrid adds
-        // into are zeroed in the output at once, beside the gridder: those writes use the
-        // device-to-host direction of the link while the gridder's reads use the other.
+        // The gridder reads the caller's complex128 visibilities in host memory, once each, while
+        // the layers no subgrid adds into are zeroed in the output beside it (those writes use the
+        // device-to-host direction of the link, the gridder's reads the other).  With w stacking
+        // the layers other than the busiest are gridded and added first and written back while the
+        // busiest one grids, so only the busiest layer's writeback follows the gridder.
         const size_t nn = nn_of(p);
         CK(p->d_layers.ensure(sizeof(float2) * nl * nn));
         std::vector<char> used(nl, 1);
+        bool split = false;
         if (wstack) {
             TRY(ensure_gaps(p));
             used.assign(p->layer_used.begin(), p->layer_used.begin() + nl);
+            TRY(ensure_layer_split(p));
+            split = p->lyr_minor_items > 0;
         }
         auto *out128 = reinterpret_cast<double2 *>(out);
+        const bool pinned = host_pinned(out, sizeof(double2) * nl * nn);
+        std::vector<size_t> stage_slot(nl, 0);  // staging layer of each used layer (pinned output)
+        size_t nused = 0;
+        for (size_t k = 0; k < nl; k++)
+            if (used[k]) stage_slot[k] = nused++;
+        if (pinned) CK(p->d_out128.ensure(sizeof(double2) * std::max<size_t>(1, nused) * nn));
+        auto stage = [&](size_t k) { return pinned ? p->d_out128.as<double2>() + stage_slot[k] * nn : nullptr; };
         CK(cudaEventRecord(p->ev_fork, p->stream));
         CK(cudaStreamWaitEvent(p->side, p->ev_fork, 0));
         for (size_t k = 0; k < nl; k++)
-            if (!used[k]) CK(launch_zero_c128(out128 + k * nn, static_cast<int64_t>(nn), p->side));
-        CK(cudaEventRecord(p->ev_join, p->side));
-        TRY(run_grid(p, vis, true, p->d_layers.as<float2>(), wstack));
-        {
+            if (!used[k]) TRY(zero_host_layer(p, out128 + k * nn, nn, pinned, p->side));
+        TRY(upload_uvw(p, uvw));  // host-to-device, beside the zero-fill
+        float2 *layers = p->d_layers.as<float2>();
+        if (!split) {
+            TRY(run_grid(p, vis, true, layers, wstack));
             StageScope t(p, P9IDG_STAGE_D2H);
             for (size_t k = 0; k < nl; k++)
                 if (used[k])
-                    CK(launch_c64_to_c128(p->d_layers.as<float2>() + k * nn, static_cast<int64_t>(nn), out128 + k * nn,
-                                          p->stream));
+                    TRY(layer_to_host(layers + k * nn, nn, out128 + k * nn, stage(k), pinned,
+                                      p->stream));
+        } else {
+            const WorkItem *items = p->d_gitems_lyr.as<WorkItem>();
+            const int32_t *subl = p->d_sub_lyr.as<int32_t>();
+            const int32_t nmi = p->lyr_minor_items, nms = p->lyr_minor_subs;
+            const size_t major = static_cast<size_t>(p->lyr_major);
+            TRY(clear_layers(p, layers, static_cast<int>(nl)));
+            TRY(grid_items(p, vis, true, items, nmi));
+            TRY(add_subgrids(p, layers, true, subl, nms));
+            CK(cudaEventRecord(p->ev_mid, p->stream));
+            CK(cudaStreamWaitEvent(p->side, p->ev_mid, 0));
+            for (size_t k = 0; k < nl; k++)
+                if (used[k] && k != major)
+                    TRY(layer_to_host(layers + k * nn, nn, out128 + k * nn, stage(k), pinned,
+                                      p->side));
+            TRY(grid_items(p, vis, true, items + nmi, static_cast<int32_t>(p->gitems_lyr.size()) - nmi));
+            TRY(add_subgrids(p, layers, true, subl + nms, static_cast<int32_t>(p->sub_lyr.size()) - nms));
+            StageScope t(p, P9IDG_STAGE_D2H);
+            TRY(layer_to_host(layers + major * nn, nn, out128 + major * nn, stage(major), pinned,
+                              p->stream));
         }
+        CK(cudaEventRecord(p->ev_join, p->side));
         CK(cudaStreamWaitEvent(p->stream, p->ev_join, 0));
         return finish_call(p);
     }
+    TRY(upload_uvw(p, uvw));
     CK(p->d_vis_in.ensure(sizeof(double2) * std::max<size_t>(1, nvis)));
     CK(p->d_layers.ensure(sizeof(float2) * nl * nn_of(p)));
     TRY(h2d(p, p->d_vis_in.p, vis, sizeof(double2) * nvis));
@@ -609,7 +794,7 @@ p9idg_status host_grid_common(p9idg_plan *p, const double *vis, const double *uv
 
 p9idg_status host_degrid_common(p9idg_plan *p, double *grid_io, const double *uvw, double *vis_out, bool wstack) {
     if (!p || !grid_io || !vis_out) return fail(P9IDG_INVALID_ARGUMENT, "null argument");
-    TRY(prepare(p, uvw));
+    TRY(prepare_state(p));
     const size_t nn = nn_of(p), nvis = vis_count_of(p);
     if (host_in_place(p)) {
         CK(p->d_grid128b.ensure(sizeof(double2) * nn));
@@ -624,6 +809,7 @@ p9idg_status host_degrid_common(p9idg_plan *p, double *grid_io, const double *uv
         CK(cudaStreamWaitEvent(p->side, p->ev_fork, 0));
         CK(cudaMemcpyAsync(grid_io, p->d_grid128b.p, sizeof(double2) * nn, cudaMemcpyDeviceToHost, p->side));
         CK(cudaEventRecord(p->ev_join, p->side));
+        TRY(upload_uvw(p, uvw));  // host-to-device, beside the copy-back of the shifted grid
         // the degridder writes the caller's complex128 output in place; uncovered samples are zeroed
         TRY(run_degrid(p, p->d_grid64.as<float2>(), true, vis_out, true, wstack, true));
         CK(cudaStreamWaitEvent(p->stream, p->ev_join, 0));
@@ -633,6 +819,7 @@ p9idg_status host_degrid_common(p9idg_plan *p, double *grid_io, const double *uv
     CK(p->d_grid128b.ensure(sizeof(double2) * nn));
     CK(p->d_grid64.ensure(sizeof(float2) * nn));
     CK(p->d_vis_out.ensure(sizeof(double2) * std::max<size_t>(1, nvis)));
+    TRY(upload_uvw(p, uvw));
     TRY(h2d(p, p->d_grid128.p, grid_io, sizeof(double2) * nn));
     {
         StageScope t(p, P9IDG_STAGE_CONVERT);
@@ -978,9 +1165,15 @@ void p9idg_plan_destroy(p9idg_plan *plan) {
         tc_release(plan->tc);
         plan->fft.release();
         plan->d_gaps.release();
+        plan->d_gitems_lyr.release();
+        plan->d_sub_lyr.release();
+        plan->d_zero128.release();
+        plan->d_uvw_prev.release();
+        plan->d_uvw_flag.release();
         if (plan->side) cudaStreamDestroy(plan->side);
         if (plan->ev_fork) cudaEventDestroy(plan->ev_fork);
         if (plan->ev_join) cudaEventDestroy(plan->ev_join);
+        if (plan->ev_mid) cudaEventDestroy(plan->ev_mid);
         if (plan->own_stream) cudaStreamDestroy(plan->own_stream);
     }
     delete plan;

@@ -172,6 +172,24 @@ __global__ void zero_c128_kernel(double2 *__restrict__ out, int64_t count) {
         out[i] = make_double2(0.0, 0.0);
 }
 
+// *flag = 1 when the two arrays of n 64-bit words differ anywhere (bitwise); *flag must be 0 before.
+__global__ void words_differ_kernel(const uint64_t *__restrict__ a, const uint64_t *__restrict__ b, int64_t n,
+                                    int32_t *flag) {
+    bool diff = false;
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+        diff |= a[i] != b[i];
+    if (__syncthreads_or(diff) && threadIdx.x == 0) *flag = 1;
+}
+
+cudaError_t launch_words_differ(const void *a, const void *b, int64_t nwords, int32_t *flag, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(flag, 0, sizeof(int32_t), st);
+    if (e != cudaSuccess || nwords == 0) return e;
+    words_differ_kernel<<<grid_blocks(nwords, 256), 256, 0, st>>>(static_cast<const uint64_t *>(a),
+                                                                  static_cast<const uint64_t *>(b), nwords, flag);
+    return cudaGetLastError();
+}
+
 // Few CTAs: this zero-fill of host memory is bound by the link and runs beside the gridder, which
 // should keep the SMs.
 cudaError_t launch_zero_c128(double2 *out, int64_t count, cudaStream_t st) {

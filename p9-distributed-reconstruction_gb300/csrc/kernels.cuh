@@ -91,6 +91,7 @@ struct SubgridOpArgs {
     bool wstack;               // AdderWStack (mirror/conjugate negative w) vs Adder
     int32_t *status;
     const int2 *refs;          // batched launches: (problem, subgrid) per block; nsub = count
+    const int32_t *sub_list;   // own launches: subgrid index per block (null: the block index)
 };
 cudaError_t launch_subgrid_ifft_add(const SubgridOpArgs &a, cudaStream_t st, const SubgridOpArgs *probs = nullptr);
 cudaError_t launch_split_subgrid_fft(const SubgridOpArgs &a, cudaStream_t st, const SubgridOpArgs *probs = nullptr);
@@ -101,6 +102,8 @@ cudaError_t launch_shift_convert(const double2 *in, int n, float2 *out64, double
 cudaError_t launch_c64_to_c128(const float2 *in, int64_t count, double2 *out, cudaStream_t st);
 cudaError_t launch_zero_ranges(double2 *out, const int64_t *ranges, int64_t nranges, cudaStream_t st);
 cudaError_t launch_zero_c128(double2 *out, int64_t count, cudaStream_t st);
+// *flag (int32, device) = whether two device arrays of nwords 64-bit words differ anywhere
+cudaError_t launch_words_differ(const void *a, const void *b, int64_t nwords, int32_t *flag, cudaStream_t st);
 cudaError_t launch_c128_to_c64(const double2 *in, int64_t count, float2 *out, cudaStream_t st);
 cudaError_t launch_unit_vis(const uint8_t *flags, int64_t count, float2 *out, cudaStream_t st);
 // sum over layers (c64 or c128 input) -> c64 grid

@@ -70,7 +70,8 @@ __device__ void load_twiddles(float2 *tw, int sign) {
     }
 }
 
-// Block -> (arguments, subgrid index): its own launch, or the (problem, subgrid) pair of a batch.
+// Block -> (arguments, subgrid index): its own launch (all subgrids, or those of a subgrid list),
+// or the (problem, subgrid) pair of a batch.
 template <bool BATCH>
 __device__ __forceinline__ const SubgridOpArgs &block_args(const SubgridOpArgs &L, const SubgridOpArgs *probs,
                                                           int &sidx) {
@@ -79,7 +80,7 @@ __device__ __forceinline__ const SubgridOpArgs &block_args(const SubgridOpArgs &
         sidx = r.y;
         return probs[r.x];
     }
-    sidx = blockIdx.x;
+    sidx = L.sub_list ? L.sub_list[blockIdx.x] : static_cast<int>(blockIdx.x);
     return L;
 }
 

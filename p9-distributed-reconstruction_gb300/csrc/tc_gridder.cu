@@ -145,7 +145,8 @@ __device__ __forceinline__ float block256_max(float v, float *red) {
 // ---------------- per-visibility coefficients (FP64 -> FP32) ----------------
 
 __global__ void tc_coef_kernel(const DevSubgrid *subs, const int64_t *coef_off, const double *uvw, const double *wn,
-                               Geometry g, float4 *coef) {
+                               Geometry g, float4 *coef, const int32_t *recompute) {
+    if (recompute && *recompute == 0) return;  // uvw bit-identical to the one coef was made from
     const DevSubgrid sg = subs[blockIdx.x];
     const double uoff = static_cast<double>(sg.u + g.S / 2 - g.N / 2) * g.uv_scale;
     const double voff = static_cast<double>(sg.v + g.S / 2 - g.N / 2) * g.uv_scale;
@@ -940,18 +941,20 @@ p9idg_status tc_prepare(TcPlanState &st, const std::vector<p9idg_subgrid> &subs,
 }
 
 // Per-visibility phase coefficients depend only on the plan and uvw: computed once and kept
-// until uvw is uploaded again (the plan clears coef_valid then).
+// until uvw is uploaded again (the plan clears coef_valid then; when it compared the new upload
+// with the previous one on the device, the kernel recomputes only if they differ).
 static p9idg_status launch_coef(TcPlanState &st, const GridderArgs &a, int32_t nsub, cudaStream_t stream,
                                 std::string &err) {
     if (nsub == 0 || st.coef_valid) return P9IDG_OK;
     tc_coef_kernel<<<nsub, 256, 0, stream>>>(a.subs, static_cast<const int64_t *>(st.coef_off), a.uvw, a.wavenumbers,
-                                             a.g, static_cast<float4 *>(st.coef));
+                                             a.g, static_cast<float4 *>(st.coef), st.coef_recompute_flag);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
         err = std::string("coefficient kernel: ") + cudaGetErrorString(e);
         return P9IDG_CUDA_ERROR;
     }
     st.coef_valid = true;
+    st.coef_recompute_flag = nullptr;
     return P9IDG_OK;
 }
 

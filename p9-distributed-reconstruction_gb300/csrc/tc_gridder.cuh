@@ -12,6 +12,9 @@ namespace p9idg {
 struct TcPlanState {
     bool ready = false;
     bool coef_valid = false;      // coefficients match the uvw now on the device
+    // Set when a new uvw upload was compared on the device with the one the coefficients were
+    // computed from: the coefficient kernel then recomputes only if this int32 flag is nonzero.
+    const int32_t *coef_recompute_flag = nullptr;
     int S = 0;
     int64_t ncoef = 0;
     void *coef = nullptr;         // float4 {du, dv, dw, 0} per gridded visibility, subgrid order

@@ -41,3 +41,46 @@ def test_in_place_equals_staged(need_gpu, mode, wstack):
         covered[s["baseline_idx"], s["time_sample_start"]:s["time_sample_start"] + s["time_sample_count"]] = True
     assert (~covered).any(), "the workload should drop some samples (quirk P1)"
     assert np.all(v1[~covered] == 0)
+
+
+def _layers_hit(part, N, S, W):
+    """w layers AdderWStack.Add writes (AdderWStack.cs:38-51), from the plan's subgrids."""
+    hit = set()
+    for s in part.plan.subgrids():
+        sx, sy, sw = int(s["u_pixel"]), int(s["v_pixel"]), int(s["w_lambda"])
+        if sw < 0:
+            sx, sy, sw = N - sx - S + 1, N - sy - S + 1, -sw - 1
+        if 1 <= sx < N - S and 1 <= sy < N - S and sw < W:
+            hit.add(sw)
+    return hit
+
+
+@pytest.mark.parametrize("mode", [pkg.MODE_FP32, pkg.MODE_TC_BF16X3], ids=["fp32", "tc_bf16x3"])
+def test_grid_w_in_place_layer_groups_and_pinned_output(need_gpu, mode):
+    """GridW in place grids the w layers other than the busiest first and writes them back while
+    the busiest one grids; page-locked outputs are written by copy engines, pageable ones by
+    kernels.  Every path must give the staged result, with unused layers exactly zero."""
+    torch = pytest.importorskip("torch")
+    obs, cd = workload("meerkat_3072", n_ant=10, nt=300, nch=16, seed=31)
+    c, cd = constants(cd, grid_size=1024)
+    part = pkg.Partitioner.CreatePartition(c, obs.uvw, obs.frequencies)
+    part.plan.set_mode(mode)
+    N, S, W = cd["grid_size"], cd["subgrid_size"], cd["wlayer_count"]
+    hit = _layers_hit(part, N, S, W)
+    assert len(hit) >= 2, "the grouping needs subgrids in more than one layer"
+    part.plan.set_host_access(0)
+    ref = pkg.IDG.GridW(c, part, obs.vis, obs.uvw, obs.frequencies)
+    part.plan.set_host_access(1)
+    for pinned in (True, False):
+        if pinned:
+            out = torch.empty((W, N, N), dtype=torch.complex128, pin_memory=True).numpy()
+        else:
+            out = np.empty((W, N, N), np.complex128)
+        for _ in range(2):  # the second call reuses the plan's grouping and staging buffers
+            out[...] = 5.0 - 3.0j
+            got = pkg.IDG.GridW(c, part, obs.vis, obs.uvw, obs.frequencies, out=out)
+            assert np.shares_memory(got, out)
+            assert rel_l2(out, ref) < 1e-6, (pinned, part.plan.host_access())
+            for k in range(W):
+                if k not in hit:
+                    assert np.all(out[k] == 0), (pinned, k)

@@ -118,3 +118,22 @@ def test_tc_unit_delta_known_answer(need_gpu, mode):
         expect = np.zeros_like(g)
         expect[pv % 128, pu % 128] = 1.0
         assert np.abs(g - expect).max() < 1e-4
+
+
+def test_tc_coefficients_follow_uvw_between_calls(need_gpu):
+    """Host calls upload uvw every time; the tensor-core coefficients are recomputed exactly when
+    the upload differs from the one they were made from (compared on the device).  A changed uvw
+    (same partition) must give the oracle's result for that uvw, and changing back the first."""
+    obs, c, cd, part, subs = _setup("small_256", dict(n_ant=8, nt=300, nch=8), pkg.MODE_TC_BF16X3)
+    uvw_b = obs.uvw * 1.0002
+    ref_a = oracle.idg_grid_w(cd, subs, obs.vis, obs.uvw, obs.frequencies)
+    ref_b = oracle.idg_grid_w(cd, subs, obs.vis, uvw_b, obs.frequencies)
+    assert rel_l2(ref_b, ref_a) > 1e-3  # the change is visible at the tolerance used below
+    for uvw, ref in [(obs.uvw, ref_a), (obs.uvw.copy(), ref_a), (uvw_b, ref_b), (uvw_b.copy(), ref_b),
+                     (obs.uvw, ref_a)]:
+        got = pkg.IDG.GridW(c, part, obs.vis, uvw, obs.frequencies)
+        assert rel_l2(got, ref) < TOL_TC
+        model = oracle.fft_forward_float(oracle.shift(obs.model_image.astype(np.float32)))
+        vis = pkg.IDG.DeGridW(c, part, model.copy(), uvw, obs.frequencies)
+        vref, _ = oracle.idg_degrid(cd, subs, model, uvw, obs.frequencies, wstack=True)
+        assert rel_l2(vis, vref) < TOL_TC
