@@ -471,9 +471,13 @@ p9idg_status grid_items(p9idg_plan *p, const void *d_vis, bool vis_c128, const W
     return P9IDG_OK;
 }
 
-// Subgrid IFFT + adder of nsub subgrids (all, or the subgrid list d_list) into the layers.
-p9idg_status add_subgrids(p9idg_plan *p, float2 *d_layers, bool wstack, const int32_t *d_list, int32_t nsub) {
+// Subgrid IFFT + adder of nsub subgrids (all, or the subgrid list d_list) into the layers,
+// after zeroing the first clear_nl layers (one timed stage either way).
+p9idg_status add_subgrids(p9idg_plan *p, float2 *d_layers, bool wstack, const int32_t *d_list, int32_t nsub,
+                          int clear_nl) {
     StageScope t(p, P9IDG_STAGE_SUBGRID_IFFT_ADD);
+    if (clear_nl > 0)
+        CK(cudaMemsetAsync(d_layers, 0, sizeof(float2) * static_cast<size_t>(clear_nl) * nn_of(p), p->stream));
     SubgridOpArgs a = subgrid_args(p);
     a.partials = p->d_partials.as<float2>();
     a.layers = d_layers;
@@ -487,17 +491,10 @@ p9idg_status add_subgrids(p9idg_plan *p, float2 *d_layers, bool wstack, const in
     return P9IDG_OK;
 }
 
-p9idg_status clear_layers(p9idg_plan *p, float2 *d_layers, int nl) {
-    StageScope t(p, P9IDG_STAGE_SUBGRID_IFFT_ADD);
-    CK(cudaMemsetAsync(d_layers, 0, sizeof(float2) * static_cast<size_t>(nl) * nn_of(p), p->stream));
-    return P9IDG_OK;
-}
-
 p9idg_status run_grid(p9idg_plan *p, const void *d_vis, bool vis_c128, float2 *d_layers, bool wstack) {
     const int nl = wstack ? p->c.wlayer_count : 1;
     TRY(grid_items(p, d_vis, vis_c128, p->d_gitems.as<WorkItem>(), static_cast<int32_t>(p->gitems.size())));
-    TRY(clear_layers(p, d_layers, nl));
-    return add_subgrids(p, d_layers, wstack, nullptr, 0);
+    return add_subgrids(p, d_layers, wstack, nullptr, 0, nl);
 }
 
 // grid (device complex64) -> vis (device, complex64 or complex128); uncovered samples are 0
@@ -764,9 +761,8 @@ p9idg_status host_grid_common(p9idg_plan *p, const double *vis, const double *uv
             const int32_t *subl = p->d_sub_lyr.as<int32_t>();
             const int32_t nmi = p->lyr_minor_items, nms = p->lyr_minor_subs;
             const size_t major = static_cast<size_t>(p->lyr_major);
-            TRY(clear_layers(p, layers, static_cast<int>(nl)));
             TRY(grid_items(p, vis, true, items, nmi));
-            TRY(add_subgrids(p, layers, true, subl, nms));
+            TRY(add_subgrids(p, layers, true, subl, nms, static_cast<int>(nl)));
             CK(cudaEventRecord(p->ev_mid, p->stream));
             CK(cudaStreamWaitEvent(p->side, p->ev_mid, 0));
             for (size_t k = 0; k < nl; k++)
@@ -774,7 +770,7 @@ p9idg_status host_grid_common(p9idg_plan *p, const double *vis, const double *uv
                     TRY(layer_to_host(layers + k * nn, nn, out128 + k * nn, stage(k), pinned,
                                       p->side));
             TRY(grid_items(p, vis, true, items + nmi, static_cast<int32_t>(p->gitems_lyr.size()) - nmi));
-            TRY(add_subgrids(p, layers, true, subl + nms, static_cast<int32_t>(p->sub_lyr.size()) - nms));
+            TRY(add_subgrids(p, layers, true, subl + nms, static_cast<int32_t>(p->sub_lyr.size()) - nms, 0));
             StageScope t(p, P9IDG_STAGE_D2H);
             TRY(layer_to_host(layers + major * nn, nn, out128 + major * nn, stage(major), pinned,
                               p->stream));
