@@ -15,13 +15,17 @@
 // run on tcgen05 with BF16 (or FP16) hi+lo operands: x ~ hi + lo, products hi*hi + hi*lo +
 // lo*hi accumulated in FP32 in tensor memory.  The P1 / T1 corrections use hi*hi only.
 //
-// Gridder MMA layout (per 8 visibilities = K16, real form, k = 2 v + re/im):
-//   A rows (192 = 3 blocks of 64, rows p*32 + y):  [A0_lo ; A0_hi ; A1_hi]
-//       p = re: [B_re, -B_im],  p = im: [B_im, B_re];  A1 = dw * A0
-//   B rows (64 = [B_lo ; B_hi], row x): [W_re, W_im] with W = vis * A_k(x)
-//   MMA2: A rows 64-191 x B rows 0-63 (M128 N64) -> TMEM cols 0..63
-//   MMA1: A rows 0-127  x B rows 32-63 (M128 N32) -> TMEM cols 0..31
-//   => P0 = D[lanes 0-63][0:32] + D[lanes 0-63][32:64],  P1 = D[lanes 64-127][32:64]
+// Gridder MMA layout (per stage of 32 visibilities = K32, k = visibility; real and imaginary
+// parts in separate rows, so two visibilities' values pack into one BF16 pair as they are):
+//   A rows (256, y = row % 32):  [Bh_re ; Bh_im ; B1_re ; B1_im ; Bl_re ; Bl_im ; 0 ; 0]
+//       B = B_k(y) = Bh + Bl,  B1 = dw_k B_k(y) (hi only)
+//   B rows (128, x = row % 32):  [Wh_re ; Wh_im ; Wl_re ; Wl_im],  W = vis_k A_k(x) = Wh + Wl
+//   MMA1: A rows 0-127 x B rows 0-127 (M128 N128) -> TMEM cols 0..127
+//   MMA2: A rows 128-255 x B rows 0-63 (M128 N64) -> TMEM cols 0..63 (rows 64-127 of it are 0)
+//   TMEM lane quarter q = (Bh+Bl)_re, (Bh+Bl)_im, B1_re, B1_im against columns
+//   [Wh_re | Wh_im | Wl_re | Wl_im]: the lo*lo block is never formed, and
+//   P0 = sum over the W column blocks of (re.re - im.im, re.im + im.re) of lanes 0-63,
+//   P1 the same of lanes 64-127.
 // Degridder (per tile of 128 visibilities = rows; k = 2x + re/im):
 //   A rows: [cos, sin](phase_A);  static B rows (192, row 2y+p):  [B0_lo ; B0_hi ; B1_hi]
 //   MMA1: A_hi x B rows 64-191 (N128) -> cols 0..127 = [T0 | T1];  MMA2: A_hi x B0_lo (N64),
@@ -100,9 +104,6 @@ __device__ __forceinline__ void split_pair(float a, float b, uint32_t &hi, uint3
     lo = Half16<BF16>::pack(a - Half16<BF16>::lo_of(hi), b - Half16<BF16>::hi_of(hi));
 }
 
-__device__ __forceinline__ uint32_t neg_hi(uint32_t w) { return w ^ 0x80000000u; }
-__device__ __forceinline__ uint32_t swap_halves(uint32_t w) { return (w >> 16) | (w << 16); }
-
 // The "memory" clobber keeps global loads from moving across these stores, so the kernels
 // prefetch the next stage's inputs into registers explicitly before storing this one.
 __device__ __forceinline__ void st_shared_v4(uint32_t addr, uint32_t a, uint32_t b, uint32_t c, uint32_t d) {
@@ -114,9 +115,14 @@ __device__ __forceinline__ void named_bar(int id, int nthreads) {
     asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
 }
 
-// byte offset of the 16-byte chunk (row, k group) in a K=64 canonical operand tile
-__device__ __forceinline__ uint32_t chunk_off(int row, int kg) {
-    return static_cast<uint32_t>((row >> 3) * 1024 + kg * 128 + (row & 7) * 16);
+// byte offset of the 16-byte chunk (row, k group) in a K=32 canonical operand tile (8-row
+// groups 512 bytes apart, k groups of 8 elements 128 bytes apart)
+__device__ __forceinline__ uint32_t chunk_off32(int row, int kg) {
+    return static_cast<uint32_t>((row >> 3) * 512 + kg * 128 + (row & 7) * 16);
+}
+
+__device__ __forceinline__ void st_shared_v2(uint32_t addr, uint32_t a, uint32_t b) {
+    asm volatile("st.shared.v2.b32 [%0], {%1, %2};" ::"r"(addr), "r"(a), "r"(b) : "memory");
 }
 
 
@@ -164,12 +170,12 @@ __global__ void tc_coef_kernel(const DevSubgrid *subs, const int64_t *coef_off, 
 
 // ---------------- gridder ----------------
 //
-// Warps 0-7 produce the MMA operands (warp = 4 visibilities of a stage = one k group; lane =
+// Warps 0-7 produce the MMA operands (warp = 4 visibilities of a stage = half a k group; lane =
 // y for the A side and x for the B side), warp 8 issues the MMAs, warp 9 streams each stage's
-// 32 coefficients and visibilities into a shared-memory ring with cp.async so the producers
-// never wait on global memory.
+// 32 coefficients and visibilities into a shared-memory ring (TMA or cp.async) so the
+// producers never wait on global memory.
 
-constexpr int kGVps = 32;      // visibilities per pipeline stage (K = 64)
+constexpr int kGVps = 32;      // visibilities per pipeline stage (K = 32)
 constexpr int kGStages = 2;
 constexpr int kGProducerWarps = 8;
 constexpr int kGMmaWarp = 8;
@@ -177,11 +183,14 @@ constexpr int kGLoaderWarp = 9;
 constexpr int kGThreads = 10 * 32;
 constexpr int kGRing = 8;                          // input ring depth (stages)
 constexpr uint32_t kGRingSlot = 32 * 16 + 32 * 16;  // coefficients + visibilities (complex128 at most)
-constexpr uint32_t kGStageA = 192 * 64 * 2;
-constexpr uint32_t kGStageB = 64 * 64 * 2;
+constexpr uint32_t kGStageA = 256 * kGVps * 2;  // MMA1 operand (rows 0-127), then MMA2's (128-255)
+constexpr uint32_t kGStageA2 = 128 * kGVps * 2;
+constexpr uint32_t kGStageB = 128 * kGVps * 2;
 constexpr uint32_t kGStageBytes = kGStageA + kGStageB;
+constexpr uint32_t kGEpilogue = 8 * 32 * 33 * 4;  // the epilogue's 8 planes reuse the stages
+static_assert(kGEpilogue <= kGStages * kGStageBytes, "epilogue planes must fit in the operand stages");
 constexpr uint32_t kGSmem = kGStages * kGStageBytes + kGRing * kGRingSlot + 512 + 1024;
-constexpr uint32_t kGTmemCols = 64;
+constexpr uint32_t kGTmemCols = 128;
 
 template <bool BF16, typename VisT, bool BATCH, bool TMA>
 __global__ void __launch_bounds__(kGThreads, 3)
@@ -228,16 +237,25 @@ __global__ void __launch_bounds__(kGThreads, 3)
         tmem_alloc(tmem_slot, kGTmemCols);
         tmem_relinquish();
     }
+    const uint32_t sbase = smem_u32(smem), rbase = smem_u32(ring);
+    if (warp < kGProducerWarps) {
+        // rows 192-255 of every stage's A operand (MMA2's lower half) stay zero
+        constexpr uint32_t kZeroBytes = 64 * kGVps * 2;
+        for (uint32_t off = threadIdx.x * 16; off < kGStages * kZeroBytes; off += kGProducerWarps * 32 * 16) {
+            const uint32_t st = off / kZeroBytes, o = off % kZeroBytes;
+            st_shared_v4(sbase + st * kGStageBytes + 192 * kGVps * 2 + o, 0u, 0u, 0u, 0u);
+        }
+        fence_proxy_async();
+    }
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
-    const uint32_t sbase = smem_u32(smem), rbase = smem_u32(ring);
 
     if (warp == kGMmaWarp) {
         // ---- MMA issuer ----
         if (lane == 0) {
-            constexpr uint32_t id32 = idesc_f16(128, 32, BF16), id64 = idesc_f16(128, 64, BF16);
+            constexpr uint32_t id128 = idesc_f16(128, 128, BF16), id64 = idesc_f16(128, 64, BF16);
             for (int i = 0; i < nstages; i++) {
                 const int s = i % kGStages;
                 const uint32_t ph = (i / kGStages) & 1;
@@ -249,11 +267,10 @@ __global__ void __launch_bounds__(kGThreads, 3)
                 tc_fence_after();
                 const uint32_t A = sbase + s * kGStageBytes, B = A + kGStageA;
 #pragma unroll
-                for (int kc = 0; kc < 4; kc++) {
-                    mma_f16(tmem, smem_desc(A + 8 * 1024 + kc * 256, 128, 1024), smem_desc(B + kc * 256, 128, 1024),
-                            id64, (i > 0 || kc > 0) ? 1u : 0u);
-                    mma_f16(tmem, smem_desc(A + kc * 256, 128, 1024), smem_desc(B + 4 * 1024 + kc * 256, 128, 1024),
-                            id32, 1u);
+                for (int kc = 0; kc < kGVps / 16; kc++) {
+                    const uint64_t db = smem_desc(B + kc * 256, 128, 512);
+                    mma_f16(tmem, smem_desc(A + kc * 256, 128, 512), db, id128, (i > 0 || kc > 0) ? 1u : 0u);
+                    mma_f16(tmem, smem_desc(A + kGStageA2 + kc * 256, 128, 512), db, id64, 1u);
                 }
                 mma_commit(&empty[s]);
             }
@@ -370,37 +387,44 @@ __global__ void __launch_bounds__(kGThreads, 3)
                 }
                 break;
             }
-            uint32_t alo_re[4], alo_im[4], ahi_re[4], ahi_im[4], a1_re[4], a1_im[4], bhi[4], blo[4];
+            // words: [pair][row] with row = Bh_re, Bh_im, B1_re, B1_im, Bl_re, Bl_im, Wh_re, Wh_im,
+            // Wl_re, Wl_im; a pair packs visibilities (2p, 2p+1) of this warp's four
+            uint32_t wd[2][10];
 #pragma unroll
-            for (int v = 0; v < 4; v++) {
-                // y side: B_k(y)
-                float sb, cb;
-                __sincosf(fmaf(c[v].y, m_y, c[v].z * g_y), &sb, &cb);
-                uint32_t hi, lo;
-                split_pair<BF16>(cb, sb, hi, lo);  // hi = (hre, him), lo = (lre, lim)
-                ahi_re[v] = neg_hi(hi);                 // (hre, -him)
-                ahi_im[v] = swap_halves(hi);            // (him, hre)
-                alo_re[v] = neg_hi(lo);
-                alo_im[v] = swap_halves(lo);
-                const float dws = c[v].z * sw;
-                const uint32_t h1 = Half16<BF16>::pack(dws * cb, dws * sb);
-                a1_re[v] = neg_hi(h1);
-                a1_im[v] = swap_halves(h1);
-                // x side: W = vis * A_k(x)
-                float sa, ca;
-                __sincosf(fmaf(c[v].x, l_x, c[v].z * f_x), &sa, &ca);
-                const float wre = (vv[v].x * ca - vv[v].y * sa) * sv, wim = (vv[v].x * sa + vv[v].y * ca) * sv;
-                split_pair<BF16>(wre, wim, bhi[v], blo[v]);
+            for (int pr = 0; pr < 2; pr++) {
+                float cb[2], sb[2], wre[2], wim[2], dws[2];
+#pragma unroll
+                for (int u = 0; u < 2; u++) {
+                    const int v = 2 * pr + u;
+                    // y side: B_k(y)
+                    __sincosf(fmaf(c[v].y, m_y, c[v].z * g_y), &sb[u], &cb[u]);
+                    dws[u] = c[v].z * sw;
+                    // x side: W = vis * A_k(x)
+                    float sa, ca;
+                    __sincosf(fmaf(c[v].x, l_x, c[v].z * f_x), &sa, &ca);
+                    wre[u] = (vv[v].x * ca - vv[v].y * sa) * sv;
+                    wim[u] = (vv[v].x * sa + vv[v].y * ca) * sv;
+                }
+                split_pair<BF16>(cb[0], cb[1], wd[pr][0], wd[pr][4]);
+                split_pair<BF16>(sb[0], sb[1], wd[pr][1], wd[pr][5]);
+                wd[pr][2] = Half16<BF16>::pack(dws[0] * cb[0], dws[1] * cb[1]);
+                wd[pr][3] = Half16<BF16>::pack(dws[0] * sb[0], dws[1] * sb[1]);
+                split_pair<BF16>(wre[0], wre[1], wd[pr][6], wd[pr][8]);
+                split_pair<BF16>(wim[0], wim[1], wd[pr][7], wd[pr][9]);
             }
+            // this warp's 4 visibilities are the (group & 1) half of k group group / 2
             const uint32_t A = sbase + s * kGStageBytes, B = A + kGStageA;
-            st_shared_v4(A + chunk_off(lane, group), alo_re[0], alo_re[1], alo_re[2], alo_re[3]);
-            st_shared_v4(A + chunk_off(32 + lane, group), alo_im[0], alo_im[1], alo_im[2], alo_im[3]);
-            st_shared_v4(A + chunk_off(64 + lane, group), ahi_re[0], ahi_re[1], ahi_re[2], ahi_re[3]);
-            st_shared_v4(A + chunk_off(96 + lane, group), ahi_im[0], ahi_im[1], ahi_im[2], ahi_im[3]);
-            st_shared_v4(A + chunk_off(128 + lane, group), a1_re[0], a1_re[1], a1_re[2], a1_re[3]);
-            st_shared_v4(A + chunk_off(160 + lane, group), a1_im[0], a1_im[1], a1_im[2], a1_im[3]);
-            st_shared_v4(B + chunk_off(lane, group), blo[0], blo[1], blo[2], blo[3]);
-            st_shared_v4(B + chunk_off(32 + lane, group), bhi[0], bhi[1], bhi[2], bhi[3]);
+            const uint32_t ko = chunk_off32(lane, group >> 1) + (group & 1) * 8;
+            st_shared_v2(A + ko, wd[0][0], wd[1][0]);                    // Bh_re: rows 0-31
+            st_shared_v2(A + 4 * 512 + ko, wd[0][1], wd[1][1]);          // Bh_im: rows 32-63
+            st_shared_v2(A + 8 * 512 + ko, wd[0][2], wd[1][2]);          // B1_re: rows 64-95
+            st_shared_v2(A + 12 * 512 + ko, wd[0][3], wd[1][3]);         // B1_im: rows 96-127
+            st_shared_v2(A + kGStageA2 + ko, wd[0][4], wd[1][4]);        // Bl_re: rows 128-159
+            st_shared_v2(A + kGStageA2 + 4 * 512 + ko, wd[0][5], wd[1][5]);  // Bl_im: rows 160-191
+            st_shared_v2(B + ko, wd[0][6], wd[1][6]);                    // Wh_re: rows 0-31
+            st_shared_v2(B + 4 * 512 + ko, wd[0][7], wd[1][7]);          // Wh_im: rows 32-63
+            st_shared_v2(B + 8 * 512 + ko, wd[0][8], wd[1][8]);          // Wl_re: rows 64-95
+            st_shared_v2(B + 12 * 512 + ko, wd[0][9], wd[1][9]);         // Wl_im: rows 96-127
             fence_proxy_async();
             __syncwarp();
             if (lane == 0) {
@@ -411,15 +435,22 @@ __global__ void __launch_bounds__(kGThreads, 3)
         // ---- epilogue: TMEM -> smem planes -> partial subgrid
         const bool ok = warp_wait(accb, 0, abort_flag, kWaitNs);
         tc_fence_after();
-        float *E = reinterpret_cast<float *>(smem);  // stage 0 is free once accb completed
-        const int q = warp & 3, half = warp >> 2;
-        const int plane = q < 2 ? q * 2 + half : (half == 1 ? 2 + q : -1);
-        if (ok && plane >= 0) {
+        float *E = reinterpret_cast<float *>(smem);  // the stages are free once accb completed
+        // warp: lane quarter q (rows (Bh+Bl)_re, (Bh+Bl)_im, B1_re, B1_im) against the real (h = 0)
+        // or imaginary (h = 1) columns of W, hi and lo blocks summed: plane 2q + h
+        const int q = warp & 3, h = warp >> 2;
+        if (ok) {
             uint32_t r[32];
-            tmem_ld32(tmem + (static_cast<uint32_t>(32 * q) << 16) + static_cast<uint32_t>(half * 32), r);
+            const uint32_t t = tmem + (static_cast<uint32_t>(32 * q) << 16) + static_cast<uint32_t>(h * 32);
+            float *e = E + (2 * q + h) * 32 * 33 + lane * 33;  // this thread's row of the plane
+            tmem_ld32(t, r);  // hi block of W
             tmem_ld_wait(r);
 #pragma unroll
-            for (int j = 0; j < 32; j++) E[plane * 32 * 33 + lane * 33 + j] = __uint_as_float(r[j]);
+            for (int j = 0; j < 32; j++) e[j] = __uint_as_float(r[j]);
+            tmem_ld32(t + 64, r);  // lo block of W
+            tmem_ld_wait(r);
+#pragma unroll
+            for (int j = 0; j < 32; j++) e[j] += __uint_as_float(r[j]);
         }
         tc_fence_before();
         named_bar(1, kGProducerWarps * 32);
@@ -431,9 +462,10 @@ __global__ void __launch_bounds__(kGThreads, 3)
                 const int p = threadIdx.x + k * kGProducerWarps * 32;
                 const int y = p >> 5, x = p & 31;
                 const int e = y * 33 + x;
-                const float p0re = (E[0 * 1056 + e] + E[1 * 1056 + e]) * i0;
-                const float p0im = (E[2 * 1056 + e] + E[3 * 1056 + e]) * i0;
-                const float p1re = E[4 * 1056 + e] * i1, p1im = E[5 * 1056 + e] * i1;
+                const float p0re = (E[0 * 1056 + e] - E[3 * 1056 + e]) * i0;
+                const float p0im = (E[1 * 1056 + e] + E[2 * 1056 + e]) * i0;
+                const float p1re = (E[4 * 1056 + e] - E[7 * 1056 + e]) * i1;
+                const float p1im = (E[5 * 1056 + e] + E[6 * 1056 + e]) * i1;
                 const float rr = ep_r[k], tap = ep_t[k];
                 const float re = fmaf(-rr, p1im, p0re), im = fmaf(rr, p1re, p0im);
                 out[((y + kS / 2) % kS) * kS + (x + kS / 2) % kS] = make_float2(re * tap, im * tap);
