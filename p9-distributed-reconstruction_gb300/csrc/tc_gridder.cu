@@ -170,8 +170,8 @@ __global__ void tc_coef_kernel(const DevSubgrid *subs, const int64_t *coef_off, 
 
 // ---------------- gridder ----------------
 //
-// Warps 0-7 produce the MMA operands (warp = 4 visibilities of a stage = half a k group; lane =
-// y for the A side and x for the B side), warp 8 issues the MMAs, warp 9 streams each stage's
+// Warps 0-7 produce the MMA operands (a lane: 4 visibilities of a stage for one row, y on the A
+// side and x on the B side), warp 8 issues the MMAs, warp 9 streams each stage's
 // 32 coefficients and visibilities into a shared-memory ring (TMA or cp.async) so the
 // producers never wait on global memory.
 
@@ -329,8 +329,13 @@ __global__ void __launch_bounds__(kGThreads, 3)
         asm volatile("cp.async.wait_all;" ::: "memory");
     } else {
         // ---- producers
-        const int group = warp;
-        const float m_y = a.lmn[lane], g_y = a.tabs[lane];  // y-side tables (l and m coincide, f and g coincide)
+        // Warps 2c and 2c+1 share k group c (8 visibilities of the stage); lanes 0-7 and 8-15 take
+        // its two halves for the same 8 rows, so every half-warp's 8-byte operand stores fall in
+        // 16 different bank pairs.  Lane: row (y, and x) yy, visibilities kv .. kv+3 of the stage.
+        const int yy = (lane & 7) + 8 * (lane >> 4) + 16 * (warp & 1);
+        const int kg = warp >> 1, kh = (lane >> 3) & 1;
+        const int kv = kg * 8 + kh * 4;
+        const float m_y = a.lmn[yy], g_y = a.tabs[yy];  // y-side tables (l and m coincide, f and g coincide)
         const float l_x = m_y, f_x = g_y;
         float ep_r[4], ep_t[4];  // remainder r and taper of the 4 pixels this thread finishes
 #pragma unroll
@@ -362,9 +367,9 @@ __global__ void __launch_bounds__(kGThreads, 3)
             float4 c[4];
             float2 vv[4];
             {
-                const float4 *rc = reinterpret_cast<const float4 *>(ring + slot * kGRingSlot) + group * 4;
+                const float4 *rc = reinterpret_cast<const float4 *>(ring + slot * kGRingSlot) + kv;
                 const int off = TMA ? static_cast<int>((v0 + i * kGVps) & 1) : 0;
-                const VisT *rv = reinterpret_cast<const VisT *>(ring + slot * kGRingSlot + 512) + off + group * 4;
+                const VisT *rv = reinterpret_cast<const VisT *>(ring + slot * kGRingSlot + 512) + off + kv;
 #pragma unroll
                 for (int v = 0; v < 4; v++) {
                     c[v] = rc[v];
@@ -374,7 +379,7 @@ __global__ void __launch_bounds__(kGThreads, 3)
                 if (TMA && i == nstages - 1) {
 #pragma unroll
                     for (int v = 0; v < 4; v++)
-                        if (i * kGVps + group * 4 + v >= nvis) vv[v] = make_float2(0.f, 0.f);
+                        if (i * kGVps + kv + v >= nvis) vv[v] = make_float2(0.f, 0.f);
                 }
             }
             // the ring slot is released only after the values read from it have been used (below):
@@ -412,9 +417,8 @@ __global__ void __launch_bounds__(kGThreads, 3)
                 split_pair<BF16>(wre[0], wre[1], wd[pr][6], wd[pr][8]);
                 split_pair<BF16>(wim[0], wim[1], wd[pr][7], wd[pr][9]);
             }
-            // this warp's 4 visibilities are the (group & 1) half of k group group / 2
             const uint32_t A = sbase + s * kGStageBytes, B = A + kGStageA;
-            const uint32_t ko = chunk_off32(lane, group >> 1) + (group & 1) * 8;
+            const uint32_t ko = chunk_off32(yy, kg) + kh * 8;
             st_shared_v2(A + ko, wd[0][0], wd[1][0]);                    // Bh_re: rows 0-31
             st_shared_v2(A + 4 * 512 + ko, wd[0][1], wd[1][1]);          // Bh_im: rows 32-63
             st_shared_v2(A + 8 * 512 + ko, wd[0][2], wd[1][2]);          // B1_re: rows 64-95

@@ -182,7 +182,9 @@ def test_empty_plan_and_stage_timing(need_gpu):
     part.plan.enable_timing(True)
     pkg.IDG.GridW(c, part, obs.vis, obs.uvw, obs.frequencies)
     t = part.plan.stage_times()
-    assert t["gridder"][1] == 1 and t["gridder"][0] > 0 and t["subgrid_ifft_add"][1] == 1
+    # one gridder + adder pass, or one per layer group when host arrays are used in place
+    n = t["gridder"][1]
+    assert n in (1, 2) and t["gridder"][0] > 0 and t["subgrid_ifft_add"][1] == n
 
 
 def test_sincos_probe(need_gpu):
