@@ -765,7 +765,7 @@ __global__ void __launch_bounds__(kDThreads, 2)
             tc_fence_after();
             const float dwe = BF16 ? c.z : c.z / a.r_scale;  // T1 was formed from r * r_scale
             const uint32_t acc = tmem + (static_cast<uint32_t>(32 * q) << 16) + static_cast<uint32_t>(b * 128);
-            float vre = 0.f, vim = 0.f;
+            float vre[2] = {0.f, 0.f}, vim[2] = {0.f, 0.f};  // even and odd rows: two independent chains
 #pragma unroll
             for (int h = 0; h < 2; h++) {
                 uint32_t t0[32], t1[32];
@@ -780,9 +780,11 @@ __global__ void __launch_bounds__(kDThreads, 2)
                     const float t1re = __uint_as_float(t1[2 * yy]), t1im = __uint_as_float(t1[2 * yy + 1]);
                     const float zre = fmaf(dwe, t1im, t0re), zim = fmaf(-dwe, t1re, t0im);
                     float sb, cb;
-                    __sincosf(fmaf(c.y, tab_m[y], c.z * tab_g[y]), &sb, &cb);
-                    vre = fmaf(cb, zre, fmaf(sb, zim, vre));
-                    vim = fmaf(cb, zim, fmaf(-sb, zre, vim));
+                    // single-plan launches: the tables are kernel parameters (constant bank)
+                    const float my = BATCH ? tab_m[y] : L.m_tab[y], gy = BATCH ? tab_g[y] : L.g_tab[y];
+                    __sincosf(fmaf(c.y, my, c.z * gy), &sb, &cb);
+                    vre[yy & 1] = fmaf(cb, zre, fmaf(sb, zim, vre[yy & 1]));
+                    vim[yy & 1] = fmaf(cb, zim, fmaf(-sb, zre, vim[yy & 1]));
                 }
             }
             tc_fence_before();
@@ -793,7 +795,7 @@ __global__ void __launch_bounds__(kDThreads, 2)
             }
             if (j < nvis) {
                 const float sc = g.inv_s2 / sq;  // exact: sq is a power of two
-                store_vis(out, j, make_float2(vre * sc, vim * sc));
+                store_vis(out, j, make_float2((vre[0] + vre[1]) * sc, (vim[0] + vim[1]) * sc));
             }
         }
     }
@@ -894,6 +896,10 @@ void fill_args(TcArgs &t, const GridderArgs &a, const TcPlanState &st) {
     t.taper = a.taper;
     t.dw_scale = st.dw_scale;
     t.r_scale = st.r_scale;
+    for (int i = 0; i < kS; i++) {
+        t.m_tab[i] = st.m_tab[i];
+        t.g_tab[i] = st.g_tab[i];
+    }
 }
 
 }  // namespace
@@ -933,6 +939,10 @@ p9idg_status tc_prepare(TcPlanState &st, const std::vector<p9idg_subgrid> &subs,
         }
     }
     st.max_w_r = wmax * kmax * rmax;
+    for (int i = 0; i < S; i++) {
+        st.m_tab[i] = lmn[i];
+        st.g_tab[i] = tabs[i];
+    }
     // powers of two keeping dw * B and r * pix inside the FP16 range (|woff| = 0, so |dw| <= k |w|)
     auto pow2_below = [](double m) {
         if (!(m > 0) || !std::isfinite(m)) return 1.f;

@@ -27,6 +27,7 @@ struct TcPlanState {
     double max_w_r = 0;           // max |dw| * max |r|: size of the neglected second-order term
     float dw_scale = 1.f;         // FP16 mode: power of two with max |dw| * dw_scale < 1
     float r_scale = 1.f;          // FP16 mode: power of two with max |r| * r_scale < 1
+    float m_tab[32] = {}, g_tab[32] = {};  // m_y and g_y (the same values serve l_x and f_x)
 };
 
 // Arguments of one problem for the tensor-core kernels.
@@ -46,6 +47,9 @@ struct TcArgs {
     int32_t *status;
     float dw_scale;  // FP16 operands: power of two bringing max |dw| below 1 (1 for BF16)
     float r_scale;   // FP16 operands: power of two bringing max |r| below 1 (1 for BF16)
+    // m_y and g_y by value: a single-plan launch reads them from the parameter bank, where the
+    // degridder's unrolled per-row loop uses them as instruction operands
+    float m_tab[32], g_tab[32];
     int32_t *done;   // batched launches: completion count / time (see GridderArgs)
     unsigned long long *finish_ns;
 };
