@@ -59,6 +59,8 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volati
 // Warp-uniform bounded wait: lane 0 polls, the outcome is broadcast, and every lane then
 // performs its own acquire on the completed phase.  All lanes must call it together.
 __device__ __forceinline__ bool warp_wait(uint64_t *bar, uint32_t parity, volatile int *abort, uint64_t limit_ns) {
+    // fast path: the phase has completed already (each lane's try_wait is its own acquire)
+    if (__all_sync(0xffffffffu, mbar_try_wait(bar, parity))) return true;
     int ok = 0;
     if ((threadIdx.x & 31) == 0) ok = mbar_wait(bar, parity, abort, limit_ns) ? 1 : 0;
     ok = __shfl_sync(0xffffffffu, ok, 0);
