@@ -234,8 +234,10 @@ p9idg_status check_params(const p9idg_params *c) {
 }
 
 // Gridder work items keep whole time samples: up to 1024 visibilities for the FP32 kernel,
-// 4096 for the tensor-core kernel (its per-item epilogue is heavier).  The subgrid list
-// records each subgrid's item slots for the subgrid IFFT + adder.
+// 4096 for the tensor-core kernel.  The tensor-core item is one FP32 accumulation in tensor
+// memory, so its length sets the rounding error: 8192 measured 1 % faster at 3072² but raised
+// the rel-L2 error against FP64 from 1.1e-5 to 2.6e-5.  The subgrid list records each
+// subgrid's item slots for the subgrid IFFT + adder.
 void build_gridder_items(p9idg_plan *p) {
     const int64_t chunk = p->gchunk > 0 ? p->gchunk : (p->mode == P9IDG_MODE_FP32 ? 1024 : 4096);
     build_work_items(p->subs, p->nch, chunk, p->dsub, p->gitems);
@@ -405,7 +407,8 @@ GridderArgs gridder_args(p9idg_plan *p) {
 
 p9idg_status ensure_tc(p9idg_plan *p) {
     if (p->tc.ready) return P9IDG_OK;
-    p->tc.degrid_chunk = p->dchunk > 0 ? p->dchunk : 4096;
+    // degridder items do not accumulate across visibilities: 8192 measured 3.5 % faster than 4096
+    p->tc.degrid_chunk = p->dchunk > 0 ? p->dchunk : 8192;
     return tc_prepare(p->tc, p->subs, p->lmn, p->c.subgrid_size, p->nch, p->wn, p->uvw.data(), p->nt, p->stream,
                       g_last_error);
 }

@@ -20,10 +20,10 @@ struct TcPlanState {
     void *coef = nullptr;         // float4 {du, dv, dw, 0} per gridded visibility, subgrid order
     void *coef_off = nullptr;     // int64 per subgrid: first coefficient of the subgrid
     void *tables = nullptr;       // float: f[S] (separable part of n), r[S*S] (remainder)
-    void *ditems = nullptr;       // degridder work items (<= 2048 visibilities)
+    void *ditems = nullptr;       // degridder work items (<= degrid_chunk visibilities)
     int32_t nditems = 0;
     std::vector<WorkItem> ditems_host;  // the same list on the host (batches merge them)
-    int64_t degrid_chunk = 4096;        // visibilities per degridder work item (set before tc_prepare)
+    int64_t degrid_chunk = 8192;        // visibilities per degridder work item (set before tc_prepare)
     double max_w_r = 0;           // max |dw| * max |r|: size of the neglected second-order term
     float dw_scale = 1.f;         // FP16 mode: power of two with max |dw| * dw_scale < 1
     float r_scale = 1.f;          // FP16 mode: power of two with max |r| * r_scale < 1
