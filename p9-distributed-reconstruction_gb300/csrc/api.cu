@@ -123,7 +123,7 @@ struct p9idg_plan {
     int32_t dchunk = 0;       // degridder visibilities per work item (0 = per-mode default)
     int64_t gridded_vis = 0;
     std::vector<float> lmn, taper;
-    std::vector<float> add_phasor;  // interleaved float2 [S][S]
+    std::vector<float> add_phasor;  // interleaved float2: [S][S] adder phasors, then S FFT twiddles
     bool taper_dirty = true;
 
     // device state
@@ -261,13 +261,18 @@ void finish_plan(p9idg_plan *p) {
     for (int y = 0; y < S; y++)
         for (int x = 0; x < S; x++) p->lmn[S + y * S + x] = compute_n(p->lmn[x], p->lmn[y]);
     p->taper.assign(S * S, 1.0f);  // CalcIdentitySpheroidal (MathFunctions.cs:69-78)
-    p->add_phasor.assign(2 * S * S, 0.f);
+    p->add_phasor.assign(2 * S * S + 2 * S, 0.f);
     for (int y = 0; y < S; y++)
         for (int x = 0; x < S; x++) {
             const double ph = kPi * static_cast<double>(x + y - S) / static_cast<double>(S);  // Adder.cs:39
             p->add_phasor[2 * (y * S + x)] = static_cast<float>(std::cos(ph));
             p->add_phasor[2 * (y * S + x) + 1] = static_cast<float>(std::sin(ph));
         }
+    for (int j = 0; j < S; j++) {  // subgrid FFT twiddles exp(+2 pi i j / S)
+        const double ph = 2 * kPi * static_cast<double>(j) / static_cast<double>(S);
+        p->add_phasor[2 * (S * S + j)] = static_cast<float>(std::cos(ph));
+        p->add_phasor[2 * (S * S + j) + 1] = static_cast<float>(std::sin(ph));
+    }
     p->wn.resize(p->nch);
     for (int i = 0; i < p->nch; i++) p->wn[i] = wavenumber(p->freq[i]);
 }
@@ -299,7 +304,7 @@ p9idg_status ensure_device(p9idg_plan *p) {
     CK(p->d_wn.ensure(sizeof(double) * std::max(1, p->nch)));
     CK(p->d_lmn.ensure(sizeof(float) * p->lmn.size()));
     CK(p->d_taper.ensure(sizeof(float) * S * S));
-    CK(p->d_phasor.ensure(sizeof(float) * 2 * S * S));
+    CK(p->d_phasor.ensure(sizeof(float) * p->add_phasor.size()));
     CK(p->d_status.ensure(sizeof(int32_t)));
     cudaStream_t st = p->stream;
     CK(cudaMemcpyAsync(p->d_wn.p, p->wn.data(), sizeof(double) * p->nch, cudaMemcpyHostToDevice, st));
@@ -419,6 +424,7 @@ SubgridOpArgs subgrid_args(p9idg_plan *p) {
     a.subs = p->d_sub.as<DevSubgrid>();
     a.nsub = static_cast<int32_t>(p->dsub.size());
     a.add_phasor = p->d_phasor.as<float2>();
+    a.twiddles = p->d_phasor.as<float2>() + static_cast<size_t>(p->c.subgrid_size) * p->c.subgrid_size;
     a.status = p->d_status.as<int32_t>();
     return a;
 }

@@ -92,6 +92,7 @@ struct SubgridOpArgs {
     int32_t *status;
     const int2 *refs;          // batched launches: (problem, subgrid) per block; nsub = count
     const int32_t *sub_list;   // own launches: subgrid index per block (null: the block index)
+    const float2 *twiddles;    // exp(+2 pi i j / S), j < S, made in FP64 (null: the kernels make them)
 };
 cudaError_t launch_subgrid_ifft_add(const SubgridOpArgs &a, cudaStream_t st, const SubgridOpArgs *probs = nullptr);
 cudaError_t launch_split_subgrid_fft(const SubgridOpArgs &a, cudaStream_t st, const SubgridOpArgs *probs = nullptr);

@@ -13,8 +13,8 @@
 //    into the read index.
 //
 // One CTA per subgrid.  The S x S transform is two passes of S-point DFTs against a
-// twiddle table in shared memory (S is 8..48, so the O(S^3) form stays in the noise
-// next to the gridder's O(vis * S^2) work).
+// twiddle table in shared memory, each split radix-4 (S is 8..48: a quarter of the O(S^3)
+// multiply-adds, against the gridder's O(vis * S^2) work).
 
 #include "kernels.cuh"
 
@@ -24,49 +24,64 @@ namespace {
 
 constexpr int kThreads = 256;
 
-template <int S>
-__device__ void dft_2d(float2 (*buf)[S + 1], float2 (*tmp)[S + 1], const float2 *tw, float scale) {
-    // rows: tmp[y][k] = sum_x buf[y][x] tw[(x k) mod S]
-    for (int i = threadIdx.x; i < S * S; i += kThreads) {
-        const int y = i / S, k = i - (i / S) * S;
-        float re = 0.f, im = 0.f;
+// One pass of the 2-D transform over S lines (ROWS: dst[y][k] = sum_x src[y][x] w^(x k); else
+// dst[k][x] = sum_y src[y][x] w^(y k)), times scale, with w = tw[1] = exp(sign 2 pi i / S).
+// Radix-4 split: with Q = S / 4 the outputs k + Q j (j < 4) of a line come from the four sums
+// P_m(k) = sum over x = m (mod 4) of a_x w^(x k) through a 4-point DFT with root w^Q = sign i,
+// so each thread makes four outputs from S complex multiply-adds.
+template <int S, bool ROWS>
+__device__ __forceinline__ void dft_pass(float2 (*src)[S + 1], float2 (*dst)[S + 1], const float2 *tw, float sign,
+                                         float scale) {
+    static_assert(S % 4 == 0, "radix-4 split needs S divisible by 4");
+    constexpr int Q = S / 4;
+    for (int t = threadIdx.x; t < S * Q; t += kThreads) {
+        const int line = t / Q, k = t - (t / Q) * Q;
+        float2 P[4] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
         int e = 0;
-#pragma unroll 8
+#pragma unroll
         for (int x = 0; x < S; x++) {
-            const float2 a = buf[y][x], w = tw[e];
-            re = fmaf(a.x, w.x, fmaf(-a.y, w.y, re));
-            im = fmaf(a.x, w.y, fmaf(a.y, w.x, im));
+            const float2 a = ROWS ? src[line][x] : src[x][line], w = tw[e];
+            P[x & 3].x = fmaf(a.x, w.x, fmaf(-a.y, w.y, P[x & 3].x));
+            P[x & 3].y = fmaf(a.x, w.y, fmaf(a.y, w.x, P[x & 3].y));
             e += k;
             if (e >= S) e -= S;
         }
-        tmp[y][k] = make_float2(re, im);
-    }
-    __syncthreads();
-    // columns: buf[k][x] = scale * sum_y tmp[y][x] tw[(y k) mod S]
-    for (int i = threadIdx.x; i < S * S; i += kThreads) {
-        const int k = i / S, x = i - (i / S) * S;
-        float re = 0.f, im = 0.f;
-        int e = 0;
-#pragma unroll 8
-        for (int y = 0; y < S; y++) {
-            const float2 a = tmp[y][x], w = tw[e];
-            re = fmaf(a.x, w.x, fmaf(-a.y, w.y, re));
-            im = fmaf(a.x, w.y, fmaf(a.y, w.x, im));
-            e += k;
-            if (e >= S) e -= S;
+        const float2 A = make_float2(P[0].x + P[2].x, P[0].y + P[2].y), B = make_float2(P[0].x - P[2].x, P[0].y - P[2].y);
+        const float2 C = make_float2(P[1].x + P[3].x, P[1].y + P[3].y);
+        const float2 D = make_float2(-sign * (P[1].y - P[3].y), sign * (P[1].x - P[3].x));  // sign i (P1 - P3)
+        const float2 X[4] = {make_float2(A.x + C.x, A.y + C.y), make_float2(B.x + D.x, B.y + D.y),
+                             make_float2(A.x - C.x, A.y - C.y), make_float2(B.x - D.x, B.y - D.y)};
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const float2 v = make_float2(X[j].x * scale, X[j].y * scale);
+            if (ROWS)
+                dst[line][k + Q * j] = v;
+            else
+                dst[k + Q * j][line] = v;
         }
-        buf[k][x] = make_float2(re * scale, im * scale);
     }
     __syncthreads();
 }
 
-// exp(sign * 2 pi i j / S), evaluated in FP64
+// S x S transform of buf in place (tmp: scratch), the sign of the twiddles given
 template <int S>
-__device__ void load_twiddles(float2 *tw, int sign) {
+__device__ void dft_2d(float2 (*buf)[S + 1], float2 (*tmp)[S + 1], const float2 *tw, float sign, float scale) {
+    dft_pass<S, true>(buf, tmp, tw, sign, 1.f);
+    dft_pass<S, false>(tmp, buf, tw, sign, scale);
+}
+
+// exp(sign * 2 pi i j / S): the plan's FP64-made table, or evaluated here in FP64
+template <int S>
+__device__ void load_twiddles(float2 *tw, int sign, const float2 *table) {
     for (int j = threadIdx.x; j < S; j += kThreads) {
-        double s, c;
-        sincospi(2.0 * j / S, &s, &c);
-        tw[j] = make_float2(static_cast<float>(c), static_cast<float>(sign * s));
+        if (table) {
+            const float2 t = table[j];
+            tw[j] = make_float2(t.x, sign * t.y);
+        } else {
+            double s, c;
+            sincospi(2.0 * j / S, &s, &c);
+            tw[j] = make_float2(static_cast<float>(c), static_cast<float>(sign * s));
+        }
     }
 }
 
@@ -116,7 +131,7 @@ __global__ void __launch_bounds__(kThreads)
         }
         sw = 0;
     }
-    load_twiddles<S>(tw, +1);
+    load_twiddles<S>(tw, +1, a.twiddles);
     // sum of the partial subgrids, in slot order
     const float2 *part = a.partials + static_cast<int64_t>(sg.item_begin) * S * S;
     for (int i = threadIdx.x; i < S * S; i += kThreads) {
@@ -129,7 +144,7 @@ __global__ void __launch_bounds__(kThreads)
         buf[i / S][i % S] = make_float2(re, im);
     }
     __syncthreads();
-    dft_2d<S>(buf, tmp, tw, static_cast<float>(1.0 / (S * S)));
+    dft_2d<S>(buf, tmp, tw, 1.f, static_cast<float>(1.0 / (S * S)));
 
     float2 *layer = a.layers + static_cast<int64_t>(sw) * N * N;
     for (int i = threadIdx.x; i < S * S; i += kThreads) {
@@ -163,7 +178,7 @@ __global__ void __launch_bounds__(kThreads)
     const bool neg = WSTACK && sg.w < 0;
     const bool in_range = WSTACK ? (sx >= 1 && sx < N - S && sy >= 1 && sy < N - S)
                                  : (sx >= 0 && sx < N - S && sy >= 0 && sy < N - S);
-    load_twiddles<S>(tw, -1);
+    load_twiddles<S>(tw, -1, a.twiddles);
     for (int i = threadIdx.x; i < S * S; i += kThreads) {
         const int y = i / S, x = i - (i / S) * S;
         float2 v = make_float2(0.f, 0.f);
@@ -183,7 +198,7 @@ __global__ void __launch_bounds__(kThreads)
         buf[(y + S / 2) % S][(x + S / 2) % S] = v;
     }
     __syncthreads();
-    dft_2d<S>(buf, tmp, tw, 1.0f);
+    dft_2d<S>(buf, tmp, tw, -1.f, 1.0f);
     float2 *out = a.subgrids + static_cast<int64_t>(sidx) * S * S;
     for (int i = threadIdx.x; i < S * S; i += kThreads) out[i] = buf[i / S][i % S];
 }
