@@ -15,7 +15,7 @@
 // run on tcgen05 with BF16 (or FP16) hi+lo operands: x ~ hi + lo, products hi*hi + hi*lo +
 // lo*hi accumulated in FP32 in tensor memory.  The P1 / T1 corrections use hi*hi only.
 //
-// Gridder MMA layout (per stage of 32 visibilities = K32, k = visibility; real and imaginary
+// Gridder MMA layout (per stage of 64 visibilities = K64, k = visibility; real and imaginary
 // parts in separate rows, so two visibilities' values pack into one BF16 pair as they are):
 //   A rows (256, y = row % 32):  [Bh_re ; Bh_im ; B1_re ; B1_im ; Bl_re ; Bl_im ; 0 ; 0]
 //       B = B_k(y) = Bh + Bl,  B1 = dw_k B_k(y) (hi only)
@@ -53,12 +53,12 @@ constexpr uint64_t kWaitNs = 2000000000ull;  // 2 s per wait before a kernel giv
 
 // Tensor maps for TMA staging (single-plan launches with complex64 visibilities in device
 // memory): coefficients as a [ncoef][4] float32 tensor, visibilities as a [nvis] 64-bit tensor
-// read 34 at a time from an even index (the TMA x coordinate must be 16-byte aligned).
+// read 66 at a time from an even index (the TMA x coordinate must be 16-byte aligned).
 struct TmaMaps {
     CUtensorMap coef;
     CUtensorMap vis;
 };
-constexpr int kVisBox = 34;
+constexpr int kVisBox = 66;
 
 // The dynamic shared memory rounded up to a 1 KB boundary by pointer arithmetic on the
 // __shared__ array itself, so that every pointer derived from it stays in the shared state
@@ -115,10 +115,10 @@ __device__ __forceinline__ void named_bar(int id, int nthreads) {
     asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
 }
 
-// byte offset of the 16-byte chunk (row, k group) in a K=32 canonical operand tile (8-row
-// groups 512 bytes apart, k groups of 8 elements 128 bytes apart)
-__device__ __forceinline__ uint32_t chunk_off32(int row, int kg) {
-    return static_cast<uint32_t>((row >> 3) * 512 + kg * 128 + (row & 7) * 16);
+// byte offset of the 16-byte chunk (row, k group) in a K=64 canonical operand tile (8-row
+// groups 1024 bytes apart, k groups of 8 elements 128 bytes apart)
+__device__ __forceinline__ uint32_t chunk_off64(int row, int kg) {
+    return static_cast<uint32_t>((row >> 3) * 1024 + kg * 128 + (row & 7) * 16);
 }
 
 __device__ __forceinline__ void st_shared_v2(uint32_t addr, uint32_t a, uint32_t b) {
@@ -170,19 +170,22 @@ __global__ void tc_coef_kernel(const DevSubgrid *subs, const int64_t *coef_off, 
 
 // ---------------- gridder ----------------
 //
-// Warps 0-7 produce the MMA operands (a lane: 4 visibilities of a stage for one row, y on the A
+// Warps 0-7 produce the MMA operands (a lane: 8 visibilities of a stage for one row, y on the A
 // side and x on the B side), warp 8 issues the MMAs, warp 9 streams each stage's
-// 32 coefficients and visibilities into a shared-memory ring (TMA or cp.async) so the
+// 64 coefficients and visibilities into a shared-memory ring (TMA or cp.async) so the
 // producers never wait on global memory.
 
-constexpr int kGVps = 32;      // visibilities per pipeline stage (K = 32)
+constexpr int kGVps = 64;      // visibilities per pipeline stage (K = 64)
 constexpr int kGStages = 2;
 constexpr int kGProducerWarps = 8;
 constexpr int kGMmaWarp = 8;
 constexpr int kGLoaderWarp = 9;
 constexpr int kGThreads = 10 * 32;
-constexpr int kGRing = 8;                          // input ring depth (stages)
-constexpr uint32_t kGRingSlot = 32 * 16 + 32 * 16;  // coefficients + visibilities (complex128 at most)
+constexpr int kGRing = 4;                                // input ring depth (stages)
+constexpr uint32_t kGRingVis = kGVps * 16;               // visibilities after the coefficients
+constexpr uint32_t kGRingSlot = kGRingVis + kGVps * 16;  // coefficients + visibilities (complex128 at most)
+constexpr uint32_t kGSbo = kGVps / 8 * 128;              // bytes between 8-row groups of an operand
+constexpr uint32_t kGRows32 = 4 * kGSbo;                 // bytes of 32 operand rows
 constexpr uint32_t kGStageA = 256 * kGVps * 2;  // MMA1 operand (rows 0-127), then MMA2's (128-255)
 constexpr uint32_t kGStageA2 = 128 * kGVps * 2;
 constexpr uint32_t kGStageB = 128 * kGVps * 2;
@@ -193,7 +196,7 @@ constexpr uint32_t kGSmem = kGStages * kGStageBytes + kGRing * kGRingSlot + 512 
 constexpr uint32_t kGTmemCols = 128;
 
 template <bool BF16, typename VisT, bool BATCH, bool TMA>
-__global__ void __launch_bounds__(kGThreads, 3)
+__global__ void __launch_bounds__(kGThreads, 2)
     tc_gridder_kernel(const TcArgs L, const TcArgs *__restrict__ probs, const __grid_constant__ TmaMaps maps) {
     extern __shared__ unsigned char smem_raw[];
     unsigned char *smem = smem_1k(smem_raw);
@@ -268,9 +271,9 @@ __global__ void __launch_bounds__(kGThreads, 3)
                 const uint32_t A = sbase + s * kGStageBytes, B = A + kGStageA;
 #pragma unroll
                 for (int kc = 0; kc < kGVps / 16; kc++) {
-                    const uint64_t db = smem_desc(B + kc * 256, 128, 512);
-                    mma_f16(tmem, smem_desc(A + kc * 256, 128, 512), db, id128, (i > 0 || kc > 0) ? 1u : 0u);
-                    mma_f16(tmem, smem_desc(A + kGStageA2 + kc * 256, 128, 512), db, id64, 1u);
+                    const uint64_t db = smem_desc(B + kc * 256, 128, kGSbo);
+                    mma_f16(tmem, smem_desc(A + kc * 256, 128, kGSbo), db, id128, (i > 0 || kc > 0) ? 1u : 0u);
+                    mma_f16(tmem, smem_desc(A + kGStageA2 + kc * 256, 128, kGSbo), db, id64, 1u);
                 }
                 mma_commit(&empty[s]);
             }
@@ -280,7 +283,7 @@ __global__ void __launch_bounds__(kGThreads, 3)
         }
         __syncwarp();
     } else if (warp == kGLoaderWarp && TMA) {
-        // ---- loader (TMA): stage i's 32 coefficients (one 2-D tile) and 34 visibilities from the
+        // ---- loader (TMA): stage i's 64 coefficients (one 2-D tile) and 66 visibilities from the
         // even index at or below the stage's first (one 1-D tile) -> ring slot i % kGRing
         if (lane == 0) {
             int issued = 0;
@@ -295,7 +298,8 @@ __global__ void __launch_bounds__(kGThreads, 3)
                 const uint32_t dst = rbase + slot * kGRingSlot;
                 mbar_expect_tx(&in_full[slot], kGVps * 16 + kVisBox * 8);
                 tma_load_2d(dst, &maps.coef, 0, static_cast<int32_t>(c0 + i * kGVps), &in_full[slot]);
-                tma_load_1d(dst + 512, &maps.vis, static_cast<int32_t>((v0 + i * kGVps) & ~int64_t(1)), &in_full[slot]);
+                tma_load_1d(dst + kGRingVis, &maps.vis, static_cast<int32_t>((v0 + i * kGVps) & ~int64_t(1)),
+                            &in_full[slot]);
                 issued = i + 1;
             }
             // tiles still in flight land before the CTA can exit (consumed ones have completed)
@@ -305,7 +309,7 @@ __global__ void __launch_bounds__(kGThreads, 3)
         }
         __syncwarp();
     } else if (warp == kGLoaderWarp) {
-        // ---- loader: stage i's 32 coefficients and visibilities -> ring slot i % kGRing
+        // ---- loader: stage i's 64 coefficients and visibilities -> ring slot i % kGRing
         for (int i = 0; i < nstages; i++) {
             const int slot = i % kGRing;
             const uint32_t ph = (i / kGRing) & 1;
@@ -316,25 +320,26 @@ __global__ void __launch_bounds__(kGThreads, 3)
                 }
                 break;
             }
-            const int j = i * kGVps + lane;
-            const bool in = j < nvis;
             const uint32_t dst = rbase + slot * kGRingSlot;
-            cp_async_16(dst + lane * 16, in ? crow + j : crow, in ? 16u : 0u);
-            if (sizeof(VisT) == 16)
-                cp_async_16(dst + 512 + lane * 16, in ? vrow + j : vrow, in ? 16u : 0u);
-            else
-                cp_async_8(dst + 512 + lane * 8, in ? vrow + j : vrow, in ? 8u : 0u);
+#pragma unroll
+            for (int h = 0; h < kGVps / 32; h++) {
+                const int q = lane + 32 * h, j = i * kGVps + q;
+                const bool in = j < nvis;
+                cp_async_16(dst + q * 16, in ? crow + j : crow, in ? 16u : 0u);
+                if (sizeof(VisT) == 16)
+                    cp_async_16(dst + kGRingVis + q * 16, in ? vrow + j : vrow, in ? 16u : 0u);
+                else
+                    cp_async_8(dst + kGRingVis + q * 8, in ? vrow + j : vrow, in ? 8u : 0u);
+            }
             cp_async_arrive(&in_full[slot]);
         }
         asm volatile("cp.async.wait_all;" ::: "memory");
     } else {
         // ---- producers
-        // Warps 2c and 2c+1 share k group c (8 visibilities of the stage); lanes 0-7 and 8-15 take
-        // its two halves for the same 8 rows, so every half-warp's 8-byte operand stores fall in
-        // 16 different bank pairs.  Lane: row (y, and x) yy, visibilities kv .. kv+3 of the stage.
-        const int yy = (lane & 7) + 8 * (lane >> 4) + 16 * (warp & 1);
-        const int kg = warp >> 1, kh = (lane >> 3) & 1;
-        const int kv = kg * 8 + kh * 4;
+        // Warp w owns k group w (visibilities 8w .. 8w+7 of the stage); lane = row (y, and x).
+        // Each lane stores one 16-byte chunk per operand row: a quarter-warp writes 128
+        // contiguous bytes, and the ring reads are broadcasts.
+        const int yy = lane, kg = warp, kv = kg * 8;
         const float m_y = a.lmn[yy], g_y = a.tabs[yy];  // y-side tables (l and m coincide, f and g coincide)
         const float l_x = m_y, f_x = g_y;
         float ep_r[4], ep_t[4];  // remainder r and taper of the 4 pixels this thread finishes
@@ -364,24 +369,6 @@ __global__ void __launch_bounds__(kGThreads, 3)
                 }
                 break;
             }
-            float4 c[4];
-            float2 vv[4];
-            {
-                const float4 *rc = reinterpret_cast<const float4 *>(ring + slot * kGRingSlot) + kv;
-                const int off = TMA ? static_cast<int>((v0 + i * kGVps) & 1) : 0;
-                const VisT *rv = reinterpret_cast<const VisT *>(ring + slot * kGRingSlot + 512) + off + kv;
-#pragma unroll
-                for (int v = 0; v < 4; v++) {
-                    c[v] = rc[v];
-                    vv[v] = load_vis(rv, v);
-                }
-                // a TMA tile past the item's end holds the next item's samples: weight them 0
-                if (TMA && i == nstages - 1) {
-#pragma unroll
-                    for (int v = 0; v < 4; v++)
-                        if (i * kGVps + kv + v >= nvis) vv[v] = make_float2(0.f, 0.f);
-                }
-            }
             // the ring slot is released only after the values read from it have been used (below):
             // an arrive right after the loads could let the next copy into the slot overtake a
             // shared-memory load still queued, which would then return the next stage's data
@@ -392,23 +379,31 @@ __global__ void __launch_bounds__(kGThreads, 3)
                 }
                 break;
             }
+            const float4 *rc = reinterpret_cast<const float4 *>(ring + slot * kGRingSlot) + kv;
+            const int off = TMA ? static_cast<int>((v0 + i * kGVps) & 1) : 0;
+            const VisT *rv = reinterpret_cast<const VisT *>(ring + slot * kGRingSlot + kGRingVis) + off + kv;
+            // a TMA tile past the item's end holds the next item's samples: weight them 0
+            const int valid = TMA ? nvis - (i * kGVps + kv) : kGVps;
             // words: [pair][row] with row = Bh_re, Bh_im, B1_re, B1_im, Bl_re, Bl_im, Wh_re, Wh_im,
-            // Wl_re, Wl_im; a pair packs visibilities (2p, 2p+1) of this warp's four
-            uint32_t wd[2][10];
+            // Wl_re, Wl_im; a pair packs visibilities (2p, 2p+1) of this warp's eight
+            uint32_t wd[4][10];
 #pragma unroll
-            for (int pr = 0; pr < 2; pr++) {
+            for (int pr = 0; pr < 4; pr++) {
                 float cb[2], sb[2], wre[2], wim[2], dws[2];
 #pragma unroll
                 for (int u = 0; u < 2; u++) {
                     const int v = 2 * pr + u;
+                    const float4 c = rc[v];
+                    float2 vv = load_vis(rv, v);
+                    if (TMA && v >= valid) vv = make_float2(0.f, 0.f);
                     // y side: B_k(y)
-                    __sincosf(fmaf(c[v].y, m_y, c[v].z * g_y), &sb[u], &cb[u]);
-                    dws[u] = c[v].z * sw;
+                    __sincosf(fmaf(c.y, m_y, c.z * g_y), &sb[u], &cb[u]);
+                    dws[u] = c.z * sw;
                     // x side: W = vis * A_k(x)
                     float sa, ca;
-                    __sincosf(fmaf(c[v].x, l_x, c[v].z * f_x), &sa, &ca);
-                    wre[u] = (vv[v].x * ca - vv[v].y * sa) * sv;
-                    wim[u] = (vv[v].x * sa + vv[v].y * ca) * sv;
+                    __sincosf(fmaf(c.x, l_x, c.z * f_x), &sa, &ca);
+                    wre[u] = (vv.x * ca - vv.y * sa) * sv;
+                    wim[u] = (vv.x * sa + vv.y * ca) * sv;
                 }
                 split_pair<BF16>(cb[0], cb[1], wd[pr][0], wd[pr][4]);
                 split_pair<BF16>(sb[0], sb[1], wd[pr][1], wd[pr][5]);
@@ -418,17 +413,19 @@ __global__ void __launch_bounds__(kGThreads, 3)
                 split_pair<BF16>(wim[0], wim[1], wd[pr][7], wd[pr][9]);
             }
             const uint32_t A = sbase + s * kGStageBytes, B = A + kGStageA;
-            const uint32_t ko = chunk_off32(yy, kg) + kh * 8;
-            st_shared_v2(A + ko, wd[0][0], wd[1][0]);                    // Bh_re: rows 0-31
-            st_shared_v2(A + 4 * 512 + ko, wd[0][1], wd[1][1]);          // Bh_im: rows 32-63
-            st_shared_v2(A + 8 * 512 + ko, wd[0][2], wd[1][2]);          // B1_re: rows 64-95
-            st_shared_v2(A + 12 * 512 + ko, wd[0][3], wd[1][3]);         // B1_im: rows 96-127
-            st_shared_v2(A + kGStageA2 + ko, wd[0][4], wd[1][4]);        // Bl_re: rows 128-159
-            st_shared_v2(A + kGStageA2 + 4 * 512 + ko, wd[0][5], wd[1][5]);  // Bl_im: rows 160-191
-            st_shared_v2(B + ko, wd[0][6], wd[1][6]);                    // Wh_re: rows 0-31
-            st_shared_v2(B + 4 * 512 + ko, wd[0][7], wd[1][7]);          // Wh_im: rows 32-63
-            st_shared_v2(B + 8 * 512 + ko, wd[0][8], wd[1][8]);          // Wl_re: rows 64-95
-            st_shared_v2(B + 12 * 512 + ko, wd[0][9], wd[1][9]);         // Wl_im: rows 96-127
+            const uint32_t ko = chunk_off64(yy, kg);
+#define P9_ST(addr, r) st_shared_v4((addr), wd[0][r], wd[1][r], wd[2][r], wd[3][r])
+            P9_ST(A + ko, 0);                              // Bh_re: rows 0-31
+            P9_ST(A + kGRows32 + ko, 1);                   // Bh_im: rows 32-63
+            P9_ST(A + 2 * kGRows32 + ko, 2);               // B1_re: rows 64-95
+            P9_ST(A + 3 * kGRows32 + ko, 3);               // B1_im: rows 96-127
+            P9_ST(A + kGStageA2 + ko, 4);                  // Bl_re: rows 128-159
+            P9_ST(A + kGStageA2 + kGRows32 + ko, 5);       // Bl_im: rows 160-191
+            P9_ST(B + ko, 6);                              // Wh_re: rows 0-31
+            P9_ST(B + kGRows32 + ko, 7);                   // Wh_im: rows 32-63
+            P9_ST(B + 2 * kGRows32 + ko, 8);               // Wl_re: rows 64-95
+            P9_ST(B + 3 * kGRows32 + ko, 9);               // Wl_im: rows 96-127
+#undef P9_ST
             fence_proxy_async();
             __syncwarp();
             if (lane == 0) {
