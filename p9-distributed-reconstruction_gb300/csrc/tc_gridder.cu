@@ -954,7 +954,7 @@ p9idg_status tc_prepare(TcPlanState &st, const std::vector<p9idg_subgrid> &subs,
               std::to_string(st.max_w_r) + ")";
         return P9IDG_UNSUPPORTED;
     }
-    // degridder work items: whole time samples, up to 4096 visibilities each
+    // degridder work items: whole time samples, up to degrid_chunk visibilities each
     std::vector<DevSubgrid> dtmp;
     std::vector<WorkItem> ditems;
     build_work_items(subs, nch, st.degrid_chunk, dtmp, ditems);
