@@ -32,7 +32,8 @@ def _problems(torch, mode):
     return out
 
 
-@pytest.mark.parametrize("mode", [pkg.MODE_FP32, pkg.MODE_TC_BF16X3], ids=["fp32", "tc_bf16x3"])
+@pytest.mark.parametrize("mode", [pkg.MODE_FP32, pkg.MODE_TC_BF16X3, pkg.MODE_TC_FP16X3],
+                         ids=["fp32", "tc_bf16x3", "tc_fp16x3"])
 def test_batch_matches_single_plans(need_gpu, mode):
     torch = pytest.importorskip("torch")
     probs = _problems(torch, mode)
