@@ -5,6 +5,7 @@
 // roofline denominator.  All are grid-stride loops sized to the SM count.
 
 #include <algorithm>
+#include <type_traits>
 
 #include "kernels.cuh"
 
@@ -61,9 +62,12 @@ __global__ void unit_vis_kernel(const uint8_t *__restrict__ flags, int64_t count
 
 template <typename T>
 __global__ void layer_sum_kernel(const T *__restrict__ layers, int nlayers, int64_t nn, float2 *__restrict__ out) {
+    // complex128 layers sum in FP64; complex64 layers in FP32 (the single-precision transform
+    // that follows dominates the rounding, and FP64 arithmetic is slow on this GPU)
+    using Acc = typename std::conditional<sizeof(T) == 16, double, float>::type;
     for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < nn;
          i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-        double re = 0, im = 0;
+        Acc re = 0, im = 0;
         for (int k = 0; k < nlayers; k++) {
             const T v = layers[static_cast<int64_t>(k) * nn + i];
             re += v.x;
@@ -73,14 +77,24 @@ __global__ void layer_sum_kernel(const T *__restrict__ layers, int nlayers, int6
     }
 }
 
-__global__ void real_part_kernel(const float2 *__restrict__ in, int n, double norm, bool shift,
+// inv_norm = 1 / norm, made on the host: a multiply instead of an FP64 division per pixel
+__global__ void real_part_kernel(const float2 *__restrict__ in, int n, double inv_norm, bool shift,
                                  float *__restrict__ outf, double *__restrict__ outd) {
     const int64_t nn = static_cast<int64_t>(n) * n;
+    const bool small = nn < (int64_t(1) << 31);  // 32-bit index arithmetic
     for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < nn;
          i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-        int r = static_cast<int>(i / n), c = static_cast<int>(i - (i / n) * n);
+        int r, c;
+        if (small) {
+            const uint32_t u = static_cast<uint32_t>(i), q = u / static_cast<uint32_t>(n);
+            r = static_cast<int>(q);
+            c = static_cast<int>(u - q * static_cast<uint32_t>(n));
+        } else {
+            r = static_cast<int>(i / n);
+            c = static_cast<int>(i - static_cast<int64_t>(r) * n);
+        }
         if (shift) shift_index(n, r, c);
-        const double v = static_cast<double>(in[static_cast<int64_t>(r) * n + c].x) / norm;
+        const double v = static_cast<double>(in[static_cast<int64_t>(r) * n + c].x) * inv_norm;
         if (outf) outf[i] = static_cast<float>(v);
         if (outd) outd[i] = v;
     }
@@ -92,12 +106,13 @@ __global__ void real_to_c64_kernel(const float *__restrict__ in, int64_t count, 
         out[i] = make_float2(in[i], 0.f);
 }
 
-__global__ void scale_c64_to_c128_kernel(const float2 *__restrict__ in, int64_t count, double norm,
+// inv_norm = 1 / norm, made on the host (the values come from a single-precision transform)
+__global__ void scale_c64_to_c128_kernel(const float2 *__restrict__ in, int64_t count, double inv_norm,
                                          double2 *__restrict__ out) {
     for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < count;
          i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
         const float2 v = in[i];
-        out[i] = make_double2(static_cast<double>(v.x) / norm, static_cast<double>(v.y) / norm);
+        out[i] = make_double2(static_cast<double>(v.x) * inv_norm, static_cast<double>(v.y) * inv_norm);
     }
 }
 
@@ -235,7 +250,8 @@ cudaError_t launch_layer_sum(const void *layers, bool c128, int nlayers, int64_t
 
 cudaError_t launch_real_part(const float2 *in, int n, double norm, bool shift, float *outf, double *outd,
                              cudaStream_t st) {
-    real_part_kernel<<<grid_blocks(static_cast<int64_t>(n) * n, 256), 256, 0, st>>>(in, n, norm, shift, outf, outd);
+    real_part_kernel<<<grid_blocks(static_cast<int64_t>(n) * n, 256), 256, 0, st>>>(in, n, 1.0 / norm, shift, outf,
+                                                                                 outd);
     return cudaGetLastError();
 }
 
@@ -245,7 +261,7 @@ cudaError_t launch_real_to_c64(const float *in, int64_t count, float2 *out, cuda
 }
 
 cudaError_t launch_scale_c64_to_c128(const float2 *in, int64_t count, double norm, double2 *out, cudaStream_t st) {
-    scale_c64_to_c128_kernel<<<grid_blocks(count, 256), 256, 0, st>>>(in, count, norm, out);
+    scale_c64_to_c128_kernel<<<grid_blocks(count, 256), 256, 0, st>>>(in, count, 1.0 / norm, out);
     return cudaGetLastError();
 }
 
