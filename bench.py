@@ -548,12 +548,18 @@ def main():
         plan.degrid_w_device(d_grid.data_ptr(), d_out.data_ptr())
 
     gridded = info["gridded_visibilities"]
+    # each rank grids its own observation (seed + rank): the job's units are the sum over ranks
+    total_gridded = gridded
+    if ws > 1:
+        tg = torch.tensor([gridded], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(tg, op=torch.distributed.ReduceOp.SUM)
+        total_gridded = int(tg.item())
     results = {}
     for mode in compare + [headline]:  # headline last: its clocks are sampled
         ms, stages, clk = time_mode(plan, pkg, mode, step, stream, args.steps, args.warmup, ws,
                                     clock_gpu=local if mode == headline else None)
         results[mode] = dict(ms=ms, stages=stages, clk=clk,
-                             value=ws * 2 * gridded * args.steps / (ms * 1e-3) / 1e6)
+                             value=2 * total_gridded * args.steps / (ms * 1e-3) / 1e6)
     head = results[headline]
     stages = head["stages"]
     launches = sum(n for (_, n) in stages.values()) - stages["h2d"][1] - stages["d2h"][1]
@@ -653,7 +659,7 @@ def main():
         h2d = nvis * 16 + 2 * obs.uvw.nbytes + N * N * 16
         d2h = W * N * N * 16 + N * N * 16 + nvis * 16
         in_place = plan.host_access()
-        e2e = {"value": ws * 2 * gridded * steps_e2e / t_e2e / 1e6, "unit": "Mvis/s",
+        e2e = {"value": 2 * total_gridded * steps_e2e / t_e2e / 1e6, "unit": "Mvis/s",
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                "host_arrays_in_place": in_place,
                "grid_w_ms": 1e3 * t_grid / steps_e2e, "degrid_w_ms": 1e3 * t_degrid / steps_e2e,
