@@ -84,3 +84,24 @@ def test_grid_w_in_place_layer_groups_and_pinned_output(need_gpu, mode):
             for k in range(W):
                 if k not in hit:
                     assert np.all(out[k] == 0), (pinned, k)
+
+
+def test_grid_non_w_in_place_pinned_output(need_gpu):
+    """Grid (one layer, no layer grouping) into page-locked and pageable outputs: copy-engine and
+    kernel writeback both give the staged result."""
+    torch = pytest.importorskip("torch")
+    obs, cd = workload("meerkat_3072", n_ant=10, nt=300, nch=16, seed=31)
+    c, cd = constants(cd, grid_size=1024)
+    part = pkg.Partitioner.CreatePartition(c, obs.uvw, obs.frequencies)
+    part.plan.set_mode(pkg.MODE_TC_BF16X3)
+    N = cd["grid_size"]
+    part.plan.set_host_access(0)
+    ref = pkg.IDG.Grid(c, part, obs.vis, obs.uvw, obs.frequencies)
+    part.plan.set_host_access(1)
+    for pinned in (True, False):
+        out = (torch.empty((N, N), dtype=torch.complex128, pin_memory=True).numpy() if pinned
+               else np.empty((N, N), np.complex128))
+        out[...] = 3.0 + 1.0j
+        got = pkg.IDG.Grid(c, part, obs.vis, obs.uvw, obs.frequencies, out=out)
+        assert np.shares_memory(got, out)
+        assert rel_l2(out, ref) < 1e-6, pinned
