@@ -524,7 +524,9 @@ def main():
     wl = synth.scaled_workload(WORKLOAD, n_ant=args.antennas, seed=synth.WORKLOADS[WORKLOAD]["obs"]["seed"] + rank)
     obs, cd = synth.build(wl)
     c = pkg.GriddingConstants.from_dict(cd)
-    part = pkg.Partitioner.CreatePartition(c, obs.uvw, obs.frequencies)
+    t_plan = time.perf_counter()
+    part = pkg.Partitioner.CreatePartition(c, obs.uvw, obs.frequencies)  # the partitioner, on the host
+    plan_ms = 1e3 * (time.perf_counter() - t_plan)
     plan = part.plan
     info = plan.info()
     headline = "tc_bf16x3" if args.mode == "auto" else args.mode
@@ -645,6 +647,8 @@ def main():
         pkg.IDG.DeGridW(c, part, h_grid, h_uvw, obs.frequencies, out=h_vout)
         steps_e2e = max(1, min(args.steps, 5))
         t_grid = t_degrid = 0.0
+        plan.reset_timing()
+        plan.enable_timing(True)  # CUDA events on the plan's stream between stages (boundary copies)
         t0 = time.perf_counter()
         for _ in range(steps_e2e):
             ta = time.perf_counter()
@@ -654,6 +658,8 @@ def main():
             t_grid += tb - ta
             t_degrid += time.perf_counter() - tb
         t_e2e = time.perf_counter() - t0
+        e2e_stages = plan.stage_times()
+        plan.enable_timing(False)
         os.sched_setaffinity(0, all_cpus)
         nvis = obs.vis.size
         h2d = nvis * 16 + 2 * obs.uvw.nbytes + N * N * 16
@@ -663,6 +669,7 @@ def main():
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                "host_arrays_in_place": in_place,
                "grid_w_ms": 1e3 * t_grid / steps_e2e, "degrid_w_ms": 1e3 * t_degrid / steps_e2e,
+               "stage_ms_per_step": {k: round(v[0] / steps_e2e, 4) for k, v in e2e_stages.items() if v[1]},
                "host_numa_local_cpus": len(local_cpus) if local_cpus else None,
                "note": "IDG.GridW + IDG.DeGridW host API, Complex(double) arrays in pinned host memory, "
                        "wall clock incl. every host<->device transfer and complex128<->complex64 conversion"
@@ -706,7 +713,8 @@ def main():
                           "gridded_visibilities": gridded, "subgrids": info["num_subgrids"],
                           "l2_flush": "inputs larger than L2 (vis 516 MB, layers 604 MB complex64)",
                           "value_counts": "gridded visibilities x 2 (gridder + degridder) per step",
-                          "layer_fft_ms": round(layer_fft_ms, 4)},
+                          "layer_fft_ms": round(layer_fft_ms, 4),
+                          "plan_ms": round(plan_ms, 1)},
                "modes": modes,
                "tc_over_fp32": (head["value"] / results["fp32"]["value"]) if "fp32" in results and
                headline != "fp32" else None,
