@@ -621,6 +621,14 @@ p9idg_status ensure_gaps(p9idg_plan *p) {
 
 bool host_in_place(const p9idg_plan *p) { return p->host_direct && p->host_access != 0; }
 
+// Work forked onto the side stream writes the caller's arrays: a call that returns early with an
+// error must not leave it running, so this waits for the side stream when it goes out of scope
+// (on success the main stream has already joined it).
+struct SideJoin {
+    p9idg_plan *p;
+    ~SideJoin() { (void)cudaStreamSynchronize(p->side); }
+};
+
 // Target w layer of each subgrid as AdderWStack.Add places it (AdderWStack.cs:38-51; -1: skipped),
 // the busiest layer by gridded time samples, and the gridder items and subgrids regrouped as
 // [every other layer | the busiest layer].  With no work outside the busiest layer there is
@@ -752,6 +760,7 @@ p9idg_status host_grid_common(p9idg_plan *p, const double *vis, const double *uv
             if (used[k]) stage_slot[k] = nused++;
         if (pinned) CK(p->d_out128.ensure(sizeof(double2) * std::max<size_t>(1, nused) * nn));
         auto stage = [&](size_t k) { return pinned ? p->d_out128.as<double2>() + stage_slot[k] * nn : nullptr; };
+        SideJoin join{p};
         CK(cudaEventRecord(p->ev_fork, p->stream));
         CK(cudaStreamWaitEvent(p->side, p->ev_fork, 0));
         for (size_t k = 0; k < nl; k++)
@@ -810,6 +819,7 @@ p9idg_status host_degrid_common(p9idg_plan *p, double *grid_io, const double *uv
                                     p->d_grid64.as<float2>(), p->d_grid128b.as<double2>(), p->stream));
         }
         // FFT.Shift(grid) mutates the caller's array (IDG.cs:24,44): copied back beside the degridder
+        SideJoin join{p};
         CK(cudaEventRecord(p->ev_fork, p->stream));
         CK(cudaStreamWaitEvent(p->side, p->ev_fork, 0));
         CK(cudaMemcpyAsync(grid_io, p->d_grid128b.p, sizeof(double2) * nn, cudaMemcpyDeviceToHost, p->side));
