@@ -52,20 +52,28 @@ class GridReducer:
         self.group = group
         self.rank = dist.get_rank(group)
         self.world_size = dist.get_world_size(group)
+        # NCCL collectives take device tensors: host arrays go through the current GPU
+        self.on_device = str(dist.get_backend(group)).lower() == "nccl"
+
+    def _to_coll(self, t):
+        return t.cuda() if self.on_device else t
+
+    def _from_coll(self, t):
+        return t.cpu() if self.on_device else t
 
     def sum_to_root(self, grid: np.ndarray, root: int = 0):
         """Host array (complex or real): the element-wise sum lands on `root` (None elsewhere)."""
-        t = _as_real_tensor(self.torch, grid).clone()
+        t = self._to_coll(_as_real_tensor(self.torch, grid).clone())
         self.dist.reduce(t, dst=root, op=self.dist.ReduceOp.SUM, group=self.group)
         if self.rank != root:
             return None
-        out = t.numpy()
+        out = self._from_coll(t).numpy()
         return out.view(grid.dtype).reshape(grid.shape) if np.iscomplexobj(grid) else out.reshape(grid.shape)
 
     def sum_all(self, grid: np.ndarray) -> np.ndarray:
-        t = _as_real_tensor(self.torch, grid).clone()
+        t = self._to_coll(_as_real_tensor(self.torch, grid).clone())
         self.dist.all_reduce(t, op=self.dist.ReduceOp.SUM, group=self.group)
-        out = t.numpy()
+        out = self._from_coll(t).numpy()
         return out.view(grid.dtype).reshape(grid.shape) if np.iscomplexobj(grid) else out.reshape(grid.shape)
 
     def sum_device_(self, tensor):
@@ -76,9 +84,9 @@ class GridReducer:
 
     def broadcast(self, arr, root: int = 0):
         """Host array from `root` to every rank (MPIMajorCycle.cs:106, 186-187, 215)."""
-        t = _as_real_tensor(self.torch, arr).clone()
+        t = self._to_coll(_as_real_tensor(self.torch, arr).clone())
         self.dist.broadcast(t, src=root, group=self.group)
-        out = t.numpy()
+        out = self._from_coll(t).numpy()
         return out.view(arr.dtype).reshape(arr.shape) if np.iscomplexobj(arr) else out.reshape(arr.shape)
 
 
