@@ -41,6 +41,70 @@ def dist_info():
     return ws, rank, local
 
 
+class NvmlClockSampler:
+    """SM clock and clock-event (throttle) reasons read through NVML every ~2 ms in a thread during
+    the timed region (read-only queries).  None when NVML cannot be loaded."""
+    NAMES = {0x8: "hw_slowdown", 0x40: "hw_thermal_slowdown", 0x20: "sw_thermal_slowdown", 0x4: "sw_power_cap"}
+
+    def __init__(self, gpu_index):
+        import ctypes
+        self.ct = ctypes
+        self.lib = ctypes.CDLL("libnvidia-ml.so.1")
+        if self.lib.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit failed")
+        self.h = ctypes.c_void_p()
+        bus = _pci_bus_id(gpu_index)  # the CUDA device's own GPU, whatever CUDA_VISIBLE_DEVICES says
+        if bus is None or self.lib.nvmlDeviceGetHandleByPciBusId_v2(bus.encode(), ctypes.byref(self.h)) != 0:
+            if self.lib.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(gpu_index), ctypes.byref(self.h)) != 0:
+                raise OSError("no NVML handle")
+        self.reasons_fn = getattr(self.lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            getattr(self.lib, "nvmlDeviceGetCurrentClocksThrottleReasons")
+        self.rows = []
+        self.stop_flag = threading.Event()
+
+    def _sample(self):
+        ct = self.ct
+        mhz, mx, rs = ct.c_uint(), ct.c_uint(), ct.c_ulonglong()
+        self.lib.nvmlDeviceGetMaxClockInfo(self.h, ct.c_int(1), ct.byref(mx))  # NVML_CLOCK_SM
+        while not self.stop_flag.is_set():
+            if self.lib.nvmlDeviceGetClockInfo(self.h, ct.c_int(1), ct.byref(mhz)) == 0 and \
+                    self.reasons_fn(self.h, ct.byref(rs)) == 0:
+                self.rows.append((mhz.value, mx.value, rs.value))
+            time.sleep(0.002)
+
+    def start(self):
+        self.t = threading.Thread(target=self._sample, daemon=True)
+        self.t.start()
+
+    def stop(self):
+        self.stop_flag.set()
+        self.t.join(timeout=5)
+        self.lib.nvmlShutdown()
+        sm = [r[0] for r in self.rows]
+        reasons = sorted({n for r in self.rows for bit, n in self.NAMES.items() if r[2] & bit})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(r[1] for r in self.rows) if self.rows else None,
+                "reasons": reasons, "samples": len(self.rows), "source": "nvml"}
+
+
+def _pci_bus_id(cuda_index):
+    """NVML's "domain:bus:device.0" id of a CUDA device, or None."""
+    try:
+        import torch
+        pr = torch.cuda.get_device_properties(cuda_index)
+        return f"{pr.pci_domain_id:08X}:{pr.pci_bus_id:02X}:{pr.pci_device_id:02X}.0"
+    except (ImportError, AttributeError, RuntimeError):
+        return None
+
+
+def clock_sampler(gpu_index):
+    """NVML sampler where the library loads, else nvidia-smi."""
+    try:
+        return NvmlClockSampler(gpu_index)
+    except (OSError, AttributeError):
+        return ClockSampler(gpu_index)
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled every 100 ms during the timed region."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -215,7 +279,7 @@ def run_cd(args):
     cd = pkg.FastSerialCD(pkg.Rectangle(0, 0, n, n), psf)
     lam, alpha, eps = 0.5, 0.2, 1e-9
     cd.Deconvolve(x0.copy(), g0.copy(), lam, alpha, 300, eps)  # warm-up: graph capture
-    clocks = ClockSampler(0)
+    clocks = clock_sampler(0)
     clocks.start()
     x, g = x0.copy(), g0.copy()
     r = cd.Deconvolve(x, g, lam, alpha, args.cd, eps)
@@ -269,7 +333,7 @@ def run_major_cycle(args):
         warm = dict(kwargs, maxMajorCycle=1, deconvIterations=min(10, kwargs["deconvIterations"]))
         pkg.MajorCycle.reconstruct_serial_cd_device(*ptrs, **warm)  # module load, FFT plans
         torch.cuda.synchronize()
-        clocks = ClockSampler(0)
+        clocks = clock_sampler(0)
         clocks.start()
         t0 = time.perf_counter()
         cycles = pkg.MajorCycle.reconstruct_serial_cd_device(*ptrs, **kwargs)
@@ -372,7 +436,7 @@ def run_batched(args):
     for _ in range(max(3, args.warmup)):
         batch.run()
     batch.synchronize()
-    clocks = ClockSampler(0)
+    clocks = clock_sampler(0)
     clocks.start()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
@@ -455,7 +519,7 @@ def time_mode(plan, pkg, mode, step, stream, steps, warmup, ws, clock_gpu=None):
     if ws > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
-    clocks = ClockSampler(clock_gpu) if clock_gpu is not None else None
+    clocks = clock_sampler(clock_gpu) if clock_gpu is not None else None
     if clocks:
         clocks.start()
     plan.reset_timing()
