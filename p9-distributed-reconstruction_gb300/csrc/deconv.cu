@@ -282,6 +282,12 @@ __global__ void __launch_bounds__(kNT, 2) cd_iter_kernel(const CdParams *pp, int
     __shared__ unsigned long long sm_in[kWarps], sm_out[kWarps];
     __shared__ CdCtl c;
     __shared__ float2 s_val;
+    // Programmatic dependent launch: this grid is launched while the previous iteration finishes
+    // (each CTA of that grid releases it as its last step) and waits here until that grid has
+    // completed and its candidates and control are visible.  Nothing the previous grid writes is
+    // read before the wait.  Releasing at the end rather than the start measured faster: early
+    // waiting CTAs cost ~2 us per iteration when most of the window lies outside the image.
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     const CdParams P = *pp;
     const int ntiles = P.tiles_x * P.tiles_y;
     const unsigned long long *kin = P.tile_key + static_cast<int64_t>(parity) * ntiles;
@@ -335,6 +341,7 @@ __global__ void __launch_bounds__(kNT, 2) cd_iter_kernel(const CdParams *pp, int
     const int ty = ty0 + static_cast<int>(blockIdx.y), tx = tx0 + static_cast<int>(blockIdx.x);
     if (ty <= ty1 && tx <= tx1) eval_tile<true>(P, P.lambda, P.alpha, ty, tx, w, &s_val, kout, vout, sm_out);
     if (lead) *cout = CdCtl{c.iter + 1, 0, 0, 0};
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");  // the next iteration may launch
 }
 
 // ------------------------------------------------------------------------------------------
@@ -730,10 +737,28 @@ p9idg_status cd_capture(p9idg_cd *cd) {
     if (cd->exec) return P9IDG_OK;
     // captured on the deconvolver's own stream (never the legacy stream); replayed on cd->stream
     const dim3 grid = cd_window_grid(cd);
+    // every launch allows programmatic serialisation with the one before it (the kernel waits on
+    // it with griddepcontrol.wait before reading its results)
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = dim3(kNT);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = cd->own;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
     CK(cudaStreamBeginCapture(cd->own, cudaStreamCaptureModeThreadLocal));
-    for (int k = 0; k < kGraphIters; k++) cd_iter_kernel<<<grid, kNT, 0, cd->own>>>(cd->params.as<CdParams>(), k & 1);
+    cudaError_t le = cudaSuccess;
+    for (int k = 0; k < kGraphIters && le == cudaSuccess; k++)
+        le = cudaLaunchKernelEx(&cfg, cd_iter_kernel, static_cast<const CdParams *>(cd->params.as<CdParams>()), k & 1);
     cudaGraph_t gph = nullptr;
-    CK(cudaStreamEndCapture(cd->own, &gph));
+    const cudaError_t ce = cudaStreamEndCapture(cd->own, &gph);
+    if (le != cudaSuccess || ce != cudaSuccess) {
+        if (gph) cudaGraphDestroy(gph);
+        return cuda_fail(le != cudaSuccess ? le : ce, "capturing the coordinate-descent graph");
+    }
     cd->graph = gph;
     CK(cudaGraphInstantiate(&cd->exec, cd->graph, 0));
     return P9IDG_OK;
