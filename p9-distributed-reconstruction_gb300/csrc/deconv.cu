@@ -134,12 +134,13 @@ struct CdParams {  // device-resident, read by every launch (so one captured gra
     int32_t pad;
 };
 
+// Max of a 64-bit key over the warp as two 32-bit hardware reductions: the high words, then the
+// low words of the lanes holding the highest one (the same lexicographic maximum).
 __device__ __forceinline__ unsigned long long warp_max(unsigned long long v) {
-    for (int o = 16; o; o >>= 1) {
-        const unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
-        v = w > v ? w : v;
-    }
-    return v;
+    const unsigned hi = static_cast<unsigned>(v >> 32);
+    const unsigned mh = __reduce_max_sync(0xffffffffu, hi);
+    const unsigned ml = __reduce_max_sync(0xffffffffu, hi == mh ? static_cast<unsigned>(v) : 0u);
+    return (static_cast<unsigned long long>(mh) << 32) | ml;
 }
 
 // Block-wide max with one barrier: every warp reduces the per-warp results itself.  sm[kWarps]
@@ -278,17 +279,29 @@ __global__ void __launch_bounds__(kNT) cd_pick_kernel(const CdParams *pp, unsign
 // (tile candidates and control) and writes buffer (k + 1) % 2: the window's tiles re-evaluated,
 // every other tile's candidate copied.  Each CTA finds the selected pixel itself from the input
 // buffer, so a launch needs no grid-wide synchronisation.
-__global__ void __launch_bounds__(kNT, 2) cd_iter_kernel(const CdParams *pp, int parity) {
+//
+// The fixed fields (state buffers, maps, sizes) are a kernel parameter captured with the graph,
+// so the first loads of a launch (the tile keys) need no pointer loaded from memory first; the
+// per-call fields (images, lambda, alpha, eps, iteration cap) come from pp, which only the host
+// writes before the graph is launched.
+__global__ void __launch_bounds__(kNT, 2) cd_iter_kernel(const __grid_constant__ CdParams F, const CdParams *pp,
+                                                         int parity) {
     __shared__ unsigned long long sm_in[kWarps], sm_out[kWarps];
     __shared__ CdCtl c;
     __shared__ float2 s_val;
+    CdParams P = F;
+    P.x = pp->x;
+    P.g = pp->g;
+    P.lambda = pp->lambda;
+    P.alpha = pp->alpha;
+    P.eps = pp->eps;
+    P.max_iter = pp->max_iter;
     // Programmatic dependent launch: this grid is launched while the previous iteration finishes
     // (each CTA of that grid releases it as its last step) and waits here until that grid has
     // completed and its candidates and control are visible.  Nothing the previous grid writes is
     // read before the wait.  Releasing at the end rather than the start measured faster: early
     // waiting CTAs cost ~2 us per iteration when most of the window lies outside the image.
     asm volatile("griddepcontrol.wait;" ::: "memory");
-    const CdParams P = *pp;
     const int ntiles = P.tiles_x * P.tiles_y;
     const unsigned long long *kin = P.tile_key + static_cast<int64_t>(parity) * ntiles;
     const float2 *vin = P.tile_val + static_cast<int64_t>(parity) * ntiles;
@@ -677,6 +690,7 @@ struct p9idg_cd {
     Buf x, g, amap, psf2, tile_key, tile_val, params, ctl, pick, word, partial, sq0, sq1, psf_tmp;
     Z2Z fft;
     CdParams hp{};
+    CdParams captured{};                   // hp as the iteration graph was captured with
     CdCtl *h_ctl = nullptr;                // pinned
     unsigned long long *h_pick = nullptr;  // pinned: selected key
     cudaGraph_t graph = nullptr;
@@ -733,8 +747,21 @@ dim3 cd_window_grid(const p9idg_cd *cd) {
     return dim3(static_cast<unsigned>(wx), static_cast<unsigned>(wy));
 }
 
+// The fields the iteration kernels take from their captured parameter (the rest come from the
+// device copy of the parameters on every launch).
+bool same_fixed_params(const CdParams &a, const CdParams &b) {
+    return a.a == b.a && a.psf2 == b.psf2 && a.tile_key == b.tile_key && a.tile_val == b.tile_val && a.ctl == b.ctl &&
+           a.n == b.n && a.ph == b.ph && a.pw == b.pw && a.tiles_x == b.tiles_x && a.tiles_y == b.tiles_y;
+}
+
 p9idg_status cd_capture(p9idg_cd *cd) {
-    if (cd->exec) return P9IDG_OK;
+    if (cd->exec) {
+        if (same_fixed_params(cd->captured, cd->hp)) return P9IDG_OK;
+        cudaGraphExecDestroy(cd->exec);
+        cudaGraphDestroy(cd->graph);
+        cd->exec = nullptr;
+        cd->graph = nullptr;
+    }
     // captured on the deconvolver's own stream (never the legacy stream); replayed on cd->stream
     const dim3 grid = cd_window_grid(cd);
     // every launch allows programmatic serialisation with the one before it (the kernel waits on
@@ -752,7 +779,8 @@ p9idg_status cd_capture(p9idg_cd *cd) {
     CK(cudaStreamBeginCapture(cd->own, cudaStreamCaptureModeThreadLocal));
     cudaError_t le = cudaSuccess;
     for (int k = 0; k < kGraphIters && le == cudaSuccess; k++)
-        le = cudaLaunchKernelEx(&cfg, cd_iter_kernel, static_cast<const CdParams *>(cd->params.as<CdParams>()), k & 1);
+        le = cudaLaunchKernelEx(&cfg, cd_iter_kernel, cd->hp, static_cast<const CdParams *>(cd->params.as<CdParams>()),
+                                k & 1);
     cudaGraph_t gph = nullptr;
     const cudaError_t ce = cudaStreamEndCapture(cd->own, &gph);
     if (le != cudaSuccess || ce != cudaSuccess) {
@@ -761,6 +789,7 @@ p9idg_status cd_capture(p9idg_cd *cd) {
     }
     cd->graph = gph;
     CK(cudaGraphInstantiate(&cd->exec, cd->graph, 0));
+    cd->captured = cd->hp;
     return P9IDG_OK;
 }
 
