@@ -116,7 +116,9 @@ __device__ __forceinline__ float prox(float x, float lipschitz, float lambda, fl
     return __fdiv_rn(num, den);
 }
 
-constexpr int kTY = 32, kTX = 128, kNT = 512, kWarps = kNT / 32;
+constexpr int kNT = 512, kWarps = kNT / 32;  // image reductions
+// coordinate descent: tiles of kTY x kTX pixels, one CTA of kCdNT threads per tile
+constexpr int kTY = 32, kTX = 128, kCdNT = 512, kCdWarps = kCdNT / 32;
 constexpr int kGraphIters = 256;  // even: every replay ends on state buffer 0
 
 struct CdCtl {  // the state one launch hands to the next
@@ -143,26 +145,26 @@ __device__ __forceinline__ unsigned long long warp_max(unsigned long long v) {
     return (static_cast<unsigned long long>(mh) << 32) | ml;
 }
 
-// Block-wide max with one barrier: every warp reduces the per-warp results itself.  sm[kWarps]
+// Block-wide max with one barrier: every warp reduces the per-warp results itself.  sm[kCdWarps]
 // must not be reused by the same CTA afterwards (each call site has its own array).
 __device__ unsigned long long block_max(unsigned long long v, unsigned long long *sm) {
-    static_assert(kWarps <= 32, "one warp reduces the per-warp results");
+    static_assert(kCdWarps <= 32, "one warp reduces the per-warp results");
     v = warp_max(v);
     if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = v;
     __syncthreads();
     const unsigned lane = threadIdx.x & 31;
-    return warp_max(lane < kWarps ? sm[lane] : 0ull);
+    return warp_max(lane < kCdWarps ? sm[lane] : 0ull);
 }
 
 // The best key over all tiles of one buffer (8 loads in flight per thread: one round up to
 // 4096 tiles, e.g. a 4096^2 image).
 __device__ unsigned long long reduce_tiles(const unsigned long long *keys, int ntiles, unsigned long long *sm) {
     unsigned long long best = 0;
-    for (int base = 0; base < ntiles; base += 8 * kNT) {
+    for (int base = 0; base < ntiles; base += 8 * kCdNT) {
         unsigned long long v[8];
 #pragma unroll
         for (int j = 0; j < 8; j++) {
-            const int t = base + j * kNT + static_cast<int>(threadIdx.x);
+            const int t = base + j * kCdNT + static_cast<int>(threadIdx.x);
             v[j] = t < ntiles ? __ldcg(keys + t) : 0ull;
         }
 #pragma unroll
@@ -182,7 +184,7 @@ struct Window {
 template <bool UPDATE>
 __device__ void eval_tile(const CdParams &P, float lambda, float alpha, int ty, int tx, const Window &w,
                           const float2 *s_val, unsigned long long *key_out, float2 *val_out, unsigned long long *sm) {
-    constexpr int R = kTY / kWarps, K = kTX / 32;
+    constexpr int R = kTY / kCdWarps, K = kTX / 32;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int yb = ty * kTY + warp * R, xb = tx * kTX + lane;
     float gv[R][K], xv[R][K], av[R][K], pv[R][K];
@@ -251,8 +253,8 @@ __device__ void eval_tile(const CdParams &P, float lambda, float alpha, int ty, 
 }
 
 // Full scan into state buffer 0: the candidate of every tile (GetAbsMax over the whole image).
-__global__ void __launch_bounds__(kNT) cd_scan_kernel(const CdParams *pp, float lambda, float alpha) {
-    __shared__ unsigned long long sm[kWarps];
+__global__ void __launch_bounds__(kCdNT) cd_scan_kernel(const CdParams *pp, float lambda, float alpha) {
+    __shared__ unsigned long long sm[kCdWarps];
     const CdParams P = *pp;
     Window w{};
     eval_tile<false>(P, lambda, alpha, blockIdx.y, blockIdx.x, w, nullptr, P.tile_key, P.tile_val, sm);
@@ -260,8 +262,8 @@ __global__ void __launch_bounds__(kNT) cd_scan_kernel(const CdParams *pp, float 
 }
 
 // The selected pixel's key and values of state buffer 0 (GetAbsMax's result), for the host.
-__global__ void __launch_bounds__(kNT) cd_pick_kernel(const CdParams *pp, unsigned long long *out_key, float2 *out_val) {
-    __shared__ unsigned long long sm[kWarps];
+__global__ void __launch_bounds__(kCdNT) cd_pick_kernel(const CdParams *pp, unsigned long long *out_key, float2 *out_val) {
+    __shared__ unsigned long long sm[kCdWarps];
     const CdParams P = *pp;
     const unsigned long long best = reduce_tiles(P.tile_key, P.tiles_x * P.tiles_y, sm);
     if (threadIdx.x == 0) {
@@ -284,9 +286,9 @@ __global__ void __launch_bounds__(kNT) cd_pick_kernel(const CdParams *pp, unsign
 // so the first loads of a launch (the tile keys) need no pointer loaded from memory first; the
 // per-call fields (images, lambda, alpha, eps, iteration cap) come from pp, which only the host
 // writes before the graph is launched.
-__global__ void __launch_bounds__(kNT, 2) cd_iter_kernel(const __grid_constant__ CdParams F, const CdParams *pp,
+__global__ void __launch_bounds__(kCdNT, 1024 / kCdNT) cd_iter_kernel(const __grid_constant__ CdParams F, const CdParams *pp,
                                                          int parity) {
-    __shared__ unsigned long long sm_in[kWarps], sm_out[kWarps];
+    __shared__ unsigned long long sm_in[kCdWarps], sm_out[kCdWarps];
     __shared__ CdCtl c;
     __shared__ float2 s_val;
     CdParams P = F;
@@ -342,7 +344,7 @@ __global__ void __launch_bounds__(kNT, 2) cd_iter_kernel(const __grid_constant__
     const int ty0 = w.y0 / kTY, ty1 = (w.y1 - 1) / kTY, tx0 = w.x0 / kTX, tx1 = (w.x1 - 1) / kTX;
     // candidates of the tiles outside the window carry over unchanged
     const int nb = gridDim.x * gridDim.y, b = blockIdx.y * gridDim.x + blockIdx.x;
-    for (int t = b + nb * static_cast<int>(threadIdx.x); t < ntiles; t += nb * kNT) {
+    for (int t = b + nb * static_cast<int>(threadIdx.x); t < ntiles; t += nb * kCdNT) {
         const int tty = t / P.tiles_x, ttx = t % P.tiles_x;
         if (tty < ty0 || tty > ty1 || ttx < tx0 || ttx > tx1) {
             kout[t] = __ldcg(kin + t);
@@ -771,7 +773,7 @@ p9idg_status cd_capture(p9idg_cd *cd) {
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = grid;
-    cfg.blockDim = dim3(kNT);
+    cfg.blockDim = dim3(kCdNT);
     cfg.dynamicSmemBytes = 0;
     cfg.stream = cd->own;
     cfg.attrs = attr;
@@ -795,7 +797,7 @@ p9idg_status cd_capture(p9idg_cd *cd) {
 
 // Candidates of every tile with (lambda, alpha) into state buffer 0, control reset.
 p9idg_status cd_scan(p9idg_cd *cd, float lambda, float alpha) {
-    cd_scan_kernel<<<dim3(cd->tiles_x, cd->tiles_y), kNT, 0, cd->stream>>>(cd->params.as<CdParams>(), lambda, alpha);
+    cd_scan_kernel<<<dim3(cd->tiles_x, cd->tiles_y), kCdNT, 0, cd->stream>>>(cd->params.as<CdParams>(), lambda, alpha);
     CK(cudaGetLastError());
     return P9IDG_OK;
 }
@@ -842,7 +844,7 @@ p9idg_status cd_abs_max(p9idg_cd *cd, const float *d_x, const float *d_g, float 
     cd->hp.g = const_cast<float *>(d_g);
     TRY(cd_upload_params(cd));
     TRY(cd_scan(cd, lambda, alpha));
-    cd_pick_kernel<<<1, kNT, 0, cd->stream>>>(cd->params.as<CdParams>(), cd->pick.as<unsigned long long>(),
+    cd_pick_kernel<<<1, kCdNT, 0, cd->stream>>>(cd->params.as<CdParams>(), cd->pick.as<unsigned long long>(),
                                              reinterpret_cast<float2 *>(cd->pick.as<unsigned long long>() + 1));
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(cd->h_pick, cd->pick.p, sizeof(unsigned long long), cudaMemcpyDeviceToHost, cd->stream));
