@@ -117,8 +117,11 @@ __device__ __forceinline__ float prox(float x, float lipschitz, float lambda, fl
 }
 
 constexpr int kNT = 512, kWarps = kNT / 32;  // image reductions
-// coordinate descent: tiles of kTY x kTX pixels, one CTA of kCdNT threads per tile
-constexpr int kTY = 32, kTX = 128, kCdNT = 512, kCdWarps = kCdNT / 32;
+// Coordinate descent: tiles of kTY x kTX pixels, one CTA of kCdNT threads per tile (8 pixels a
+// thread).  A 768^2 update window (a 384^2 PSF) spans 21 x 7 = 147 such tiles, one CTA per SM of
+// the 152, each evaluating 5,120 pixels; 32 x 128 tiles of 512 threads need 175 CTAs, two on some
+// SMs, and the 3072^2 major cycle's coordinate descent ran 19 % slower with them.
+constexpr int kTY = 40, kTX = 128, kCdNT = 640, kCdWarps = kCdNT / 32, kCdBlocksPerSM = 1;
 constexpr int kGraphIters = 256;  // even: every replay ends on state buffer 0
 
 struct CdCtl {  // the state one launch hands to the next
@@ -286,7 +289,7 @@ __global__ void __launch_bounds__(kCdNT) cd_pick_kernel(const CdParams *pp, unsi
 // so the first loads of a launch (the tile keys) need no pointer loaded from memory first; the
 // per-call fields (images, lambda, alpha, eps, iteration cap) come from pp, which only the host
 // writes before the graph is launched.
-__global__ void __launch_bounds__(kCdNT, 1024 / kCdNT) cd_iter_kernel(const __grid_constant__ CdParams F, const CdParams *pp,
+__global__ void __launch_bounds__(kCdNT, kCdBlocksPerSM) cd_iter_kernel(const __grid_constant__ CdParams F, const CdParams *pp,
                                                          int parity) {
     __shared__ unsigned long long sm_in[kCdWarps], sm_out[kCdWarps];
     __shared__ CdCtl c;
