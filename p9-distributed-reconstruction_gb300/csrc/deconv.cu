@@ -186,10 +186,15 @@ struct Window {
 // memory latency rather than one per pixel.
 template <bool UPDATE>
 __device__ void eval_tile(const CdParams &P, float lambda, float alpha, int ty, int tx, const Window &w,
-                          const float2 *s_val, unsigned long long *key_out, float2 *val_out, unsigned long long *sm) {
+                          const float2 *sel_val, unsigned long long *key_out, float2 *val_out,
+                          unsigned long long *sm) {
     constexpr int R = kTY / kCdWarps, K = kTX / 32;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int yb = ty * kTY + warp * R, xb = tx * kTX + lane;
+    // the selected pixel's (new, current) values: every thread loads them beside its pixels (one
+    // request per warp), so no block barrier is needed to share them
+    float2 sv = make_float2(0.0f, 0.0f);
+    if (UPDATE) sv = __ldcg(sel_val);
     float gv[R][K], xv[R][K], av[R][K], pv[R][K];
 #pragma unroll
     for (int r = 0; r < R; r++) {
@@ -212,10 +217,9 @@ __device__ void eval_tile(const CdParams &P, float lambda, float alpha, int ty, 
         }
     }
     float xnew = 0.0f, xdiff = 0.0f;
-    if (UPDATE) {  // the selected pixel's values, loaded by thread 0 while the loads above were issued
-        __syncthreads();
-        xnew = s_val->x;
-        xdiff = __fsub_rn(s_val->y, s_val->x);  // pixelOld - maxPixel.PixelNew
+    if (UPDATE) {
+        xnew = sv.x;
+        xdiff = __fsub_rn(sv.y, sv.x);  // pixelOld - maxPixel.PixelNew
     }
     unsigned long long best = 0;
     float bnew = 0.0f, bold = 0.0f;
@@ -293,7 +297,6 @@ __global__ void __launch_bounds__(kCdNT, kCdBlocksPerSM) cd_iter_kernel(const __
                                                          int parity) {
     __shared__ unsigned long long sm_in[kCdWarps], sm_out[kCdWarps];
     __shared__ CdCtl c;
-    __shared__ float2 s_val;
     CdParams P = F;
     P.x = pp->x;
     P.g = pp->g;
@@ -354,10 +357,9 @@ __global__ void __launch_bounds__(kCdNT, kCdBlocksPerSM) cd_iter_kernel(const __
             vout[t] = __ldcg(vin + t);
         }
     }
-    if (threadIdx.x == 0)
-        s_val = __ldcg(vin + static_cast<int>(w.py / kTY) * P.tiles_x + static_cast<int>(w.px / kTX));
+    const float2 *sel_val = vin + static_cast<int>(w.py / kTY) * P.tiles_x + static_cast<int>(w.px / kTX);
     const int ty = ty0 + static_cast<int>(blockIdx.y), tx = tx0 + static_cast<int>(blockIdx.x);
-    if (ty <= ty1 && tx <= tx1) eval_tile<true>(P, P.lambda, P.alpha, ty, tx, w, &s_val, kout, vout, sm_out);
+    if (ty <= ty1 && tx <= tx1) eval_tile<true>(P, P.lambda, P.alpha, ty, tx, w, sel_val, kout, vout, sm_out);
     if (lead) *cout = CdCtl{c.iter + 1, 0, 0, 0};
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");  // the next iteration may launch
 }
