@@ -293,8 +293,8 @@ __global__ void __launch_bounds__(kCdNT) cd_pick_kernel(const CdParams *pp, unsi
 // so the first loads of a launch (the tile keys) need no pointer loaded from memory first; the
 // per-call fields (images, lambda, alpha, eps, iteration cap) come from pp, which only the host
 // writes before the graph is launched.
-__global__ void __launch_bounds__(kCdNT, kCdBlocksPerSM) cd_iter_kernel(const __grid_constant__ CdParams F, const CdParams *pp,
-                                                         int parity) {
+__global__ void __launch_bounds__(kCdNT, kCdBlocksPerSM)
+    cd_iter_kernel(const __grid_constant__ CdParams F, const CdParams *pp, int parity) {
     __shared__ unsigned long long sm_in[kCdWarps], sm_out[kCdWarps];
     __shared__ CdCtl c;
     CdParams P = F;
