@@ -78,12 +78,15 @@ def test_tc_rejects_other_subgrid_sizes():
     assert e.value.code == 8
 
 
-@pytest.mark.parametrize("mode", MODES)
-@pytest.mark.parametrize("nch,nt,N,chunks", [
+EDGE_SHAPES = [
     (1, 37, 256, None),       # one channel: work items far from a multiple of the 32 / 128 tiles
     (3, 301, 255, None),      # odd grid size, odd channel count
     (16, 120, 512, (2048, 2048)),  # small work items: several partial subgrids per subgrid
-])
+]
+
+
+@pytest.mark.parametrize("mode", MODES)
+@pytest.mark.parametrize("nch,nt,N,chunks", EDGE_SHAPES)
 def test_tc_edge_shapes(need_gpu, mode, nch, nt, N, chunks):
     obs, cd = workload("small_256", n_ant=9, nt=nt, nch=nch, seed=nch * 100 + nt)
     c, cd = constants(cd, grid_size=N)
@@ -100,6 +103,38 @@ def test_tc_edge_shapes(need_gpu, mode, nch, nt, N, chunks):
     vis = pkg.IDG.DeGridW(c, part, model.copy(), obs.uvw, obs.frequencies)
     ref, _ = oracle.idg_degrid(cd, subs, model, obs.uvw, obs.frequencies, wstack=True)
     assert rel_l2(vis, ref) < TOL_TC
+
+
+@pytest.mark.parametrize("mode", MODES)
+@pytest.mark.parametrize("nch,nt,N,chunks", EDGE_SHAPES)
+def test_tc_edge_shapes_device(need_gpu, mode, nch, nt, N, chunks):
+    """The same shapes through the device API with complex64 visibilities, the single-plan path
+    that stages inputs with TMA: a stage's visibility tile starts at the even index at or below
+    its first sample, and the samples past a work item's end (the next item's) weigh nothing."""
+    torch = pytest.importorskip("torch")
+    obs, cd = workload("small_256", n_ant=9, nt=nt, nch=nch, seed=nch * 100 + nt)
+    c, cd = constants(cd, grid_size=N)
+    part = pkg.Partitioner.CreatePartition(c, obs.uvw, obs.frequencies)
+    plan = part.plan
+    plan.set_mode(mode)
+    if chunks:
+        pkg.set_chunking(plan, *chunks)
+    subs = oracle.partition(cd, obs.uvw, obs.frequencies)
+    W = cd["wlayer_count"]
+    d_vis = torch.from_numpy(obs.vis.astype(np.complex64)).cuda()
+    d_layers = torch.empty((W, N, N), dtype=torch.complex64, device="cuda")
+    plan.grid_w_device(d_vis.data_ptr(), d_layers.data_ptr())
+    plan.synchronize()
+    ref = oracle.idg_grid_w(cd, subs, obs.vis, obs.uvw, obs.frequencies)
+    assert rel_l2(d_layers.cpu().numpy(), ref) < TOL_TC
+    rng = np.random.default_rng(N)
+    model = rng.standard_normal((N, N)) + 1j * rng.standard_normal((N, N))
+    d_grid = torch.from_numpy(model.astype(np.complex64)).cuda()
+    d_out = torch.empty_like(d_vis)
+    plan.degrid_w_device(d_grid.data_ptr(), d_out.data_ptr())
+    plan.synchronize()
+    ref_v, _ = oracle.idg_degrid(cd, subs, model, obs.uvw, obs.frequencies, wstack=True)
+    assert rel_l2(d_out.cpu().numpy(), ref_v) < TOL_TC
 
 
 @pytest.mark.parametrize("mode", MODES)
