@@ -45,7 +45,7 @@ def test_maps_match_oracle(need_gpu, n, p):
 
 @pytest.mark.parametrize("n,p,lam,alpha,iters,eps", [
     (64, 8, 0.4, 0.2, 300, 1e-5),
-    (200, 24, 1.0, 0.05, 500, 1e-5),     # image not a multiple of the 32 x 128 tiles
+    (200, 24, 1.0, 0.05, 500, 1e-5),     # image not a multiple of the 128-pixel tile width
     (256, 64, 0.5, 0.2, 400, 1e-6),      # window spans several tiles in both directions
     (96, 96, 0.5, 0.2, 300, 1e-5),       # full PSF: the window covers the whole image
     (512, 16, 0.2, 0.1, 1500, 1e-7),     # many graph replays
@@ -59,6 +59,27 @@ def test_deconvolve_bit_exact_vs_oracle(need_gpu, n, p, lam, alpha, iters, eps):
     r = cd.Deconvolve(x, g, lam, alpha, iters, eps)
     assert (r.Converged, r.IterationCount) == (oconv, oit)
     assert oit > 0
+    assert x.tobytes() == ox.tobytes()
+    assert g.tobytes() == og.tobytes()
+    cd.destroy()
+
+
+def test_deconvolve_bit_exact_with_windows_inside_the_image(need_gpu):
+    """A 1024^2 gradient map that peaks near the centre and a 160^2 PSF: the 320^2 update
+    windows lie inside the image and span whole rows and columns of tiles, as on a real sky in
+    the major cycle (the other cases mostly clip their windows at the image edges)."""
+    n, p = 1024, 160
+    psf, x0, g0 = _problem(n, p, seed=17)
+    yy, xx = np.mgrid[:n, :n] - n // 2
+    g0 = (g0 * np.exp(-(yy ** 2 + xx ** 2) / (2 * 120.0 ** 2))).astype(np.float32)
+    cd = _cd(n, psf)
+    psf2, amap = cd.maps()
+    ox, og, oconv, oit = oracle.deconvolve(x0, g0, amap, psf2, 0.3, 0.1, 400, 1e-7)
+    x, g = x0.copy(), g0.copy()
+    r = cd.Deconvolve(x, g, 0.3, 0.1, 400, 1e-7)
+    assert (r.Converged, r.IterationCount) == (oconv, oit) and oit > 100
+    changed = np.argwhere(x != x0)
+    assert len(changed) > 0 and np.all((changed >= p) & (changed < n - p))  # windows inside
     assert x.tobytes() == ox.tobytes()
     assert g.tobytes() == og.tobytes()
     cd.destroy()
