@@ -11,14 +11,16 @@
 // Coordinate descent.  One iteration of FastSerialCD picks the pixel whose proximal update
 // changes it most (a scan of the whole image), sets it, and adds the scaled PSF^2 to the
 // gradient map in a window around it.  Only pixels in that window change, so the GPU keeps
-// the best candidate of every 32x128 tile and, per iteration, re-evaluates only the tiles the
-// window touches: one launch reduces the tile candidates the previous launch left to the
+// the best candidate of every 40 x 128 tile and, per iteration, re-evaluates only the tiles
+// the window touches: one launch reduces the tile candidates the previous launch left to the
 // selected pixel (every CTA does this itself), updates the window's gradients and writes those
-// tiles' new candidates into the other of two state buffers.  A candidate is one 64-bit key, (|change| bits << 32) | (0xFFFFFFFF - pixel index),
-// so the largest key is the largest change and, among equal changes, the first pixel, which is
-// the order in which GetAbsMax (FastSerialCD.cs:135-170) keeps its winner.  Iterations are
-// launched from a captured CUDA graph, 256 at a time; a launch after the stopping iteration
-// does nothing, so the iteration count and result equal the reference's loop.
+// tiles' new candidates into the other of two state buffers.  A candidate is one 64-bit key,
+// (|change| bits << 32) | (0xFFFFFFFF - pixel index), so the largest key is the largest change
+// and, among equal changes, the first pixel, which is the order in which GetAbsMax
+// (FastSerialCD.cs:135-170) keeps its winner.  Iterations are launched from a captured CUDA
+// graph, 256 at a time, each chained to the previous by programmatic dependent launch; a launch
+// after the stopping iteration does nothing, so the iteration count and result equal the
+// reference's loop.
 
 #include <cuda_runtime.h>
 #include <cufft.h>
