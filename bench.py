@@ -265,6 +265,32 @@ def run_reference(args):
     return 0
 
 
+def link_rates(nbytes=256 << 20, reps=3):
+    """This machine's host-link rates (GB/s): copies of nbytes between device memory and page-locked
+    host memory, best of reps after one warm-up.  The e2e figure moves its bytes over this link, so
+    the rates say whether a low e2e comes from the box."""
+    import torch
+
+    d = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    h = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    s = torch.cuda.current_stream()
+    out = {}
+    for name, copy in (("h2d", lambda: d.copy_(h, non_blocking=True)),
+                       ("d2h", lambda: h.copy_(d, non_blocking=True))):
+        best = 0.0
+        for i in range(reps + 1):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(s)
+            copy()
+            e1.record(s)
+            e1.synchronize()
+            if i:
+                best = max(best, nbytes / (e0.elapsed_time(e1) * 1e-3) / 1e9)
+        out[name] = round(best, 1)
+    out["bytes"] = nbytes
+    return out
+
+
 def run_cd(args):
     """FastSerialCD alone at the 3072^2 workload's sizes: a 3072^2 image and a 384^2 PSF (cut 8,
     so a 768^2 PSF^2 window); a seeded synthetic PSF (Gaussian main lobe + noise sidelobes) and
@@ -694,6 +720,7 @@ def main():
         local_cpus = gpu_local_cpus(local)
         if local_cpus:
             os.sched_setaffinity(0, local_cpus)
+        link = link_rates()
         pin = lambda shape, dt: torch.empty(shape, dtype=dt, pin_memory=True).numpy()  # noqa: E731
         h_vis = pin(obs.vis.shape, torch.complex128)
         h_vis[...] = obs.vis
@@ -735,6 +762,7 @@ def main():
                "grid_w_ms": 1e3 * t_grid / steps_e2e, "degrid_w_ms": 1e3 * t_degrid / steps_e2e,
                "stage_ms_per_step": {k: round(v[0] / steps_e2e, 4) for k, v in e2e_stages.items() if v[1]},
                "host_numa_local_cpus": len(local_cpus) if local_cpus else None,
+               "link_gbs": link,
                "note": "IDG.GridW + IDG.DeGridW host API, Complex(double) arrays in pinned host memory, "
                        "wall clock incl. every host<->device transfer and complex128<->complex64 conversion"
                        + ("; the kernels read the visibilities and the model grid and write the degridded "
