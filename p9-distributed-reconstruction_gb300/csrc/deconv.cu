@@ -702,6 +702,7 @@ struct p9idg_cd {
     CdParams captured{};                   // hp as the iteration graph was captured with
     CdCtl *h_ctl = nullptr;                // pinned
     unsigned long long *h_pick = nullptr;  // pinned: selected key
+    cudaEvent_t ev_ctl = nullptr;          // the control word of a replay has reached h_ctl
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
 };
@@ -809,12 +810,6 @@ p9idg_status cd_scan(p9idg_cd *cd, float lambda, float alpha) {
     return P9IDG_OK;
 }
 
-p9idg_status cd_read_ctl(p9idg_cd *cd) {
-    CK(cudaMemcpyAsync(cd->h_ctl, cd->ctl.p, sizeof(CdCtl), cudaMemcpyDeviceToHost, cd->stream));
-    CK(cudaStreamSynchronize(cd->stream));
-    return P9IDG_OK;
-}
-
 // FastSerialCD.Deconvolve on device buffers x, g (n x n float), in place.
 p9idg_status cd_run(p9idg_cd *cd, float *d_x, float *d_g, float lambda, float alpha, int32_t max_iter, float eps,
                     p9idg_cd_result *res) {
@@ -828,12 +823,19 @@ p9idg_status cd_run(p9idg_cd *cd, float *d_x, float *d_g, float lambda, float al
     TRY(cd_upload_params(cd));
     TRY(cd_scan(cd, lambda, alpha));
     TRY(cd_capture(cd));
+    // One replay stays in flight while the host reads the control word the previous one left: the
+    // copy after replay r is enqueued before replay r + 1, so the GPU never waits on the host.  A
+    // replay launched after the stopping one does nothing (every launch sees the done flag).
     const int64_t max_replays = static_cast<int64_t>(std::max(max_iter, 0)) / kGraphIters + 2;
+    CK(cudaGraphLaunch(cd->exec, cd->stream));
     for (int64_t r = 0; r < max_replays; r++) {
-        CK(cudaGraphLaunch(cd->exec, cd->stream));
-        TRY(cd_read_ctl(cd));
+        CK(cudaMemcpyAsync(cd->h_ctl, cd->ctl.p, sizeof(CdCtl), cudaMemcpyDeviceToHost, cd->stream));
+        CK(cudaEventRecord(cd->ev_ctl, cd->stream));
+        if (r + 1 < max_replays) CK(cudaGraphLaunch(cd->exec, cd->stream));
+        CK(cudaEventSynchronize(cd->ev_ctl));
         if (cd->h_ctl->done) break;
     }
+    CK(cudaStreamSynchronize(cd->stream));  // the replay in flight, if any
     if (!cd->h_ctl->done) return fail(P9IDG_DEVICE_CHECK_FAILED, "coordinate descent did not stop");
     if (cd->h_ctl->error)
         return fail(P9IDG_INVALID_ARGUMENT,
@@ -863,6 +865,7 @@ p9idg_status cd_abs_max(p9idg_cd *cd, const float *d_x, const float *d_g, float 
 
 void cd_release(p9idg_cd *cd) {
     if (cd->stream) cudaStreamSynchronize(cd->stream);
+    if (cd->ev_ctl) cudaEventDestroy(cd->ev_ctl);
     if (cd->exec) cudaGraphExecDestroy(cd->exec);
     if (cd->graph) cudaGraphDestroy(cd->graph);
     Buf *bufs[] = {&cd->x, &cd->g, &cd->amap, &cd->psf2, &cd->tile_key, &cd->tile_val, &cd->params, &cd->ctl,
@@ -880,6 +883,7 @@ p9idg_status cd_init(p9idg_cd *cd, int n, const float *psf, int h, int w) {
     cd->stream = cd->own;
     CK(cudaMallocHost(reinterpret_cast<void **>(&cd->h_ctl), sizeof(CdCtl)));
     CK(cudaMallocHost(reinterpret_cast<void **>(&cd->h_pick), sizeof(unsigned long long)));
+    CK(cudaEventCreateWithFlags(&cd->ev_ctl, cudaEventDisableTiming));
     cd->n = n;
     cd->tiles_x = (n + kTX - 1) / kTX;
     cd->tiles_y = (n + kTY - 1) / kTY;
