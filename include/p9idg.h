@@ -51,6 +51,17 @@ enum {
     P9IDG_MODE_TC_FP16X3 = 2  /* tensor cores, FP16 hi+lo split (3 products), FP32 accumulation */
 };
 
+/* Largest |dw * r(x, y)| the tensor-core modes accept.  They write the reference's phasor
+ * exp(i dw n(x, y)) (Gridder.cs:61-67) as A(x) B(y) exp(i dw r(x, y)), with r the non-separable
+ * remainder of the n table (centred on zero), and expand the last factor to first order; the
+ * term left out is at most (dw r)^2 / 2 = 5e-5 of each visibility's contribution at this limit,
+ * inside the modes' stated 1e-4 relative-L2 bound together with their rounding (~1e-5).  A plan
+ * whose gridded samples exceed it keeps the FP32 kernels when a tensor-core mode is selected
+ * (p9idg_plan_set_mode returns P9IDG_OK, p9idg_plan_info.mode stays P9IDG_MODE_FP32 and
+ * p9idg_last_error() says why); a call whose uvw exceeds it on a tensor-core plan returns
+ * P9IDG_UNSUPPORTED. */
+#define P9IDG_TC_MAX_W_TERM 0.01
+
 /* GriddingConstants (Core/ImageDomainGridder/GriddingConstants.cs:33-52).
  * scale_arcsec is the cell size in radians, stored as float like the
  * reference's ScaleArcSec.  WStepLambda is not a field: the reference never
@@ -89,7 +100,10 @@ typedef struct p9idg_plan_info {
     int64_t gridded_visibilities;  /* visibilities covered by subgrids (the partitioner drops some) */
     int64_t work_items;            /* (subgrid, time-chunk) units the gridder kernels process */
     int32_t nbl, nt, nch;
-    int32_t mode;
+    int32_t mode;                  /* the kernels the plan runs (P9IDG_MODE_*) */
+    int32_t requested_mode;        /* the mode last passed to p9idg_plan_set_mode */
+    double tc_w_term;              /* max |dw| * max |r| of the plan's samples (vs P9IDG_TC_MAX_W_TERM);
+                                      -1 until a tensor-core mode has been requested */
 } p9idg_plan_info;
 
 /* ---------------- plans: Partitioner ---------------- */
@@ -110,7 +124,8 @@ p9idg_status p9idg_plan_num_subgrids(const p9idg_plan *plan, int64_t *n);
 /* Copies the subgrid list (reference order: baseline-major, then time). */
 p9idg_status p9idg_plan_get_subgrids(const p9idg_plan *plan, p9idg_subgrid *out, int64_t capacity);
 p9idg_status p9idg_plan_get_info(const p9idg_plan *plan, p9idg_plan_info *out);
-/* Selects the gridder/degridder kernels (P9IDG_MODE_*). */
+/* Selects the gridder/degridder kernels (P9IDG_MODE_*).  A tensor-core mode on a plan whose
+ * w term exceeds P9IDG_TC_MAX_W_TERM keeps the FP32 kernels (see there). */
 p9idg_status p9idg_plan_set_mode(p9idg_plan *plan, int32_t mode);
 /* Subgrid taper float[S][S] applied by gridder and degridder (GriddingConstants.SubgridSpheroidal,
  * Gridder.cs:76,111); NULL restores the identity taper the reference uses. */
@@ -194,8 +209,11 @@ p9idg_status p9idg_synchronize(p9idg_plan *plan);
  *   d_vis       device complex64[nbl][nt][nch];  d_layers: device complex64[W][N][N], overwritten
  * Subgrid sizes 8, 16, 24, 32, 48 only.  Synchronous: returns after the GPU work on cuda_stream
  * (NULL = legacy default stream) has finished.  The first call on a device looks up the array's
- * address; make it before any stream capture.  All calls share the array: calls whose GPU work
- * overlaps race and must be ordered by the caller. */
+ * address; make it before any stream capture.  Under CUDA's lazy module loading (the default,
+ * CUDA_MODULE_LOADING=LAZY) the array is committed on a device by that first call, not when the
+ * library loads: a caller with a fixed start-up reservation makes one warm-up call then (nsub = 0
+ * only clears d_layers).  All calls share the array: calls whose GPU work overlaps race and must
+ * be ordered by the caller. */
 p9idg_status p9idg_grid_w_device_noalloc(const p9idg_params *c, const p9idg_subgrid *d_subgrids, int64_t nsub,
                                          const double *d_uvw, int32_t nbl, int32_t nt, const double *frequencies,
                                          int32_t nch, const void *d_vis, void *d_layers, void *cuda_stream);

@@ -48,7 +48,12 @@ class SubgridC(ctypes.Structure):
 class PlanInfo(ctypes.Structure):
     _fields_ = [("num_subgrids", ctypes.c_int64), ("input_visibilities", ctypes.c_int64),
                 ("gridded_visibilities", ctypes.c_int64), ("work_items", ctypes.c_int64),
-                ("nbl", ctypes.c_int32), ("nt", ctypes.c_int32), ("nch", ctypes.c_int32), ("mode", ctypes.c_int32)]
+                ("nbl", ctypes.c_int32), ("nt", ctypes.c_int32), ("nch", ctypes.c_int32), ("mode", ctypes.c_int32),
+                ("requested_mode", ctypes.c_int32), ("tc_w_term", ctypes.c_double)]
+
+
+# Largest |dw r| the tensor-core modes accept (P9IDG_TC_MAX_W_TERM)
+TC_MAX_W_TERM = 0.01
 
 
 # name -> (restype, argtypes); every symbol include/p9idg.h declares

@@ -113,6 +113,8 @@ struct p9idg_plan {
     p9idg_params c{};
     int32_t nbl = 0, nt = 0, nch = 0;
     int32_t mode = P9IDG_MODE_FP32;
+    int32_t requested_mode = P9IDG_MODE_FP32;
+    double tc_w_term = -1;  // max |dw| * max |r| of the plan's samples, once a tensor-core mode was asked for
     std::vector<double> freq, wn, uvw;
     std::vector<p9idg_subgrid> subs;
     std::vector<DevSubgrid> dsub;
@@ -392,6 +394,9 @@ p9idg_status finish_call(p9idg_plan *p) {
     CK(cudaMemcpyAsync(&status, p->d_status.p, sizeof(int32_t), cudaMemcpyDeviceToHost, p->stream));
     CK(cudaStreamSynchronize(p->stream));
     if (p->timing) collect_timing(p);
+    if (status == kStatusWTerm)
+        return fail(P9IDG_UNSUPPORTED, "this call's uvw puts |dw r| above P9IDG_TC_MAX_W_TERM for the tensor-core "
+                                       "form: use P9IDG_MODE_FP32 or a plan made from this uvw");
     if (status != 0)
         return fail(P9IDG_DEVICE_CHECK_FAILED, "a kernel bounds check tripped (status " + std::to_string(status) + ")");
     return P9IDG_OK;
@@ -1098,6 +1103,8 @@ p9idg_status p9idg_plan_get_info(const p9idg_plan *plan, p9idg_plan_info *out) {
     out->nt = plan->nt;
     out->nch = plan->nch;
     out->mode = plan->mode;
+    out->requested_mode = plan->requested_mode;
+    out->tc_w_term = plan->tc_w_term;
     return P9IDG_OK;
 }
 
@@ -1109,6 +1116,18 @@ p9idg_status p9idg_plan_set_mode(p9idg_plan *plan, int32_t mode) {
         return fail(P9IDG_UNSUPPORTED, "subgrid size not supported by the FP32 kernels");
     if (mode != P9IDG_MODE_FP32 && !tc_subgrid_size_supported(plan->c.subgrid_size))
         return fail(P9IDG_UNSUPPORTED, "subgrid size not supported by the tensor-core kernels");
+    plan->requested_mode = mode;
+    if (mode != P9IDG_MODE_FP32) {
+        if (plan->tc_w_term < 0)
+            plan->tc_w_term = tc_w_term(plan->subs, plan->lmn, plan->c.subgrid_size, plan->wn, plan->uvw.data(),
+                                        plan->nt);
+        if (!(plan->tc_w_term <= P9IDG_TC_MAX_W_TERM)) {
+            // outside the first-order form's error bound: the FP32 kernels grid this plan
+            g_last_error = "tensor-core mode not used: |dw r| = " + std::to_string(plan->tc_w_term) + " > " +
+                           std::to_string(P9IDG_TC_MAX_W_TERM) + " for this plan; it runs the FP32 kernels";
+            mode = P9IDG_MODE_FP32;
+        }
+    }
     const bool regroup = (plan->mode == P9IDG_MODE_FP32) != (mode == P9IDG_MODE_FP32);
     plan->mode = mode;
     if (regroup) build_gridder_items(plan);

@@ -102,6 +102,10 @@ extern "C" p9idg_status p9idg_autotune(const p9idg_params *c, const double *uvw,
         }
         p9idg_plan_info info{};
         p9idg_plan_get_info(plan, &info);
+        if (info.mode != mode) {  // a tensor-core mode this sample's w term rules out
+            p9idg_plan_destroy(plan);
+            continue;
+        }
         void *stream = nullptr;
         for (int gc : gchunks)
             for (int dc : dchunks) {

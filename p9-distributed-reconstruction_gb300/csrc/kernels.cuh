@@ -8,7 +8,9 @@
 namespace p9idg {
 
 // Device status word bits set by kernels whose own checks trip (the access is skipped).
-enum : int32_t { kStatusIndex = 1, kStatusWait = 2 };
+// kStatusWTerm: a tensor-core call's uvw put |dw r| above P9IDG_TC_MAX_W_TERM (the plan's own
+// uvw was checked when the mode was selected; this catches a different uvw passed to a call)
+enum : int32_t { kStatusIndex = 1, kStatusWait = 2, kStatusWTerm = 4 };
 
 // FFT.Shift (FFT.cs:221-264) as an index map on a square [n][n] array: the quadrant swap
 // of the leading 2*(n/2) rows/columns; for odd n the last row and column stay in place.

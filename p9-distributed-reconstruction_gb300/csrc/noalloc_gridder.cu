@@ -9,9 +9,13 @@
 // in one file-scope __device__ array of fixed size instead.
 //
 // Limits and sharing:
-//  * kNoAllocScratchBytes (32 MiB) is reserved on every GPU that loads this library,
-//    for the life of the process.  The subgrids are processed in batches that fit it;
-//    subgrid sizes above 48 and more than 64 channels are rejected.
+//  * kNoAllocScratchBytes (32 MiB) is held on every GPU that loads this library's device
+//    code, for the life of the process.  Under CUDA's lazy module loading (the default) that
+//    happens at the first call on a device (the cudaGetSymbolAddress below), not when the
+//    library is loaded: a caller with a fixed start-up reservation makes one warm-up call
+//    (nsub = 0) at start-up.  The subgrids are processed in batches that fit the array
+//    (4,077 subgrids at S = 32, 1,816 at S = 48); subgrid sizes above 48 and more than 64
+//    channels are rejected.
 //  * All calls share the array and it keeps the previous call's contents.  Every
 //    scratch word a batch reads is written earlier in the same batch, and the status
 //    word is cleared at the start of each call.  Calls whose GPU work overlaps (on

@@ -3,10 +3,12 @@
 // The per-subgrid phase of the reference (Gridder.cs:61-67, 143-145) is
 //     phi_k(x, y) = du_k l_x + dv_k m_y + dw_k n(x, y)
 // with n the reference's FP32 ComputeN table.  Writing n = f(x) + g(y) + r(x, y), with
-// f(x) = n(l_x, 0), g(y) = n(0, m_y) (the same table) and r the small remainder
-// (~ -l^2 m^2), the phasor factorises as A_k(x) B_k(y) exp(i dw_k r(x, y)) with
+// f(x) = n(l_x, 0) + c/2, g(y) = n(0, m_y) + c/2 (the same table) and r the small remainder
+// (~ l^2 m^2 / 4) less the constant c that centres its range on zero (halving max |r|), the
+// phasor factorises as A_k(x) B_k(y) exp(i dw_k r(x, y)) with
 // A_k(x) = exp(i(du_k l_x + dw_k f_x)), B_k(y) = exp(i(dv_k m_y + dw_k g_y)).  To first
-// order in dw r (|dw r| <= ~1e-3 here, second order ~5e-7):
+// order in dw r (|dw r| <= P9IDG_TC_MAX_W_TERM = 0.01 is enforced, so the term left out is
+// <= 5e-5 of each visibility's contribution; ~5e-4 at the 3072^2 workload, ~1e-7 left out):
 //   gridder:   P[y][x] = sum_k vis_k A B (1 + i dw_k r) = P0 + i r (.) P1,
 //              P0 = B diag(vis) A^T,  P1 = B diag(vis dw) A^T          (rank-K updates)
 //   degridder: vis_k = 1/S^2 sum_y conj(B_k(y)) [T0_k(y) - i dw_k T1_k(y)],
@@ -150,8 +152,11 @@ __device__ __forceinline__ float block256_max(float v, float *red) {
 
 // ---------------- per-visibility coefficients (FP64 -> FP32) ----------------
 
+// dw_limit = P9IDG_TC_MAX_W_TERM / max |r|: a visibility with a larger |dw| (possible only when a
+// call passes a uvw other than the plan's, which was checked on the host) sets kStatusWTerm.
 __global__ void tc_coef_kernel(const DevSubgrid *subs, const int64_t *coef_off, const double *uvw, const double *wn,
-                               Geometry g, float4 *coef, const int32_t *recompute) {
+                               Geometry g, float4 *coef, const int32_t *recompute, double dw_limit,
+                               int32_t *status) {
     if (recompute && *recompute == 0) return;  // uvw bit-identical to the one coef was made from
     const DevSubgrid sg = subs[blockIdx.x];
     const double uoff = static_cast<double>(sg.u + g.S / 2 - g.N / 2) * g.uv_scale;
@@ -159,13 +164,17 @@ __global__ void tc_coef_kernel(const DevSubgrid *subs, const int64_t *coef_off, 
     const double woff = 2 * kPi * (static_cast<double>(g.wstep_lambda) * (static_cast<double>(sg.w) + 0.5));
     const int nvis = sg.nt * g.nch;
     float4 *out = coef + coef_off[blockIdx.x];
+    bool over = false;
     for (int j = threadIdx.x; j < nvis; j += blockDim.x) {
         const int t = sg.t0 + j / g.nch, ch = j - (j / g.nch) * g.nch;
         const double *q = uvw + (static_cast<int64_t>(sg.bl) * g.nt_all + t) * 3;
         const double k = wn[ch];
+        const double dw = woff - k * q[2];
+        over |= !(fabs(dw) <= dw_limit);
         out[j] = make_float4(static_cast<float>(uoff - k * q[0]), static_cast<float>(voff - k * q[1]),
-                             static_cast<float>(woff - k * q[2]), 0.f);
+                             static_cast<float>(dw), 0.f);
     }
+    if (over) atomicOr(status, kStatusWTerm);
 }
 
 // ---------------- gridder ----------------
@@ -903,6 +912,63 @@ void fill_args(TcArgs &t, const GridderArgs &a, const TcPlanState &st) {
 
 bool tc_subgrid_size_supported(int S) { return S == kS; }
 
+namespace {
+
+// The separable part f (S floats, serving as f(x) and g(y)) and the remainder r (S*S floats) of
+// the reference's FP32 n table (Gridder.cs:168-174 values in lmn[S..]): f(x) = n(l_x, 0) + c/2
+// and r = n - f(x) - f(y), where the constant c centres the range of r on zero.  Returns max |r|.
+double separable_tables(const std::vector<float> &lmn, int S, std::vector<float> &tabs) {
+    tabs.assign(S + S * S, 0.f);
+    std::vector<double> f0(S);
+    for (int x = 0; x < S; x++) {
+        const double l = lmn[x], t = l * l;
+        f0[x] = t / (t + std::sqrt(1.0 - t));
+    }
+    double rlo = INFINITY, rhi = -INFINITY;
+    for (int y = 0; y < S; y++)
+        for (int x = 0; x < S; x++) {
+            const double r = static_cast<double>(lmn[S + y * S + x]) - static_cast<float>(f0[x]) -
+                             static_cast<float>(f0[y]);
+            rlo = std::min(rlo, r);
+            rhi = std::max(rhi, r);
+        }
+    const double c = 0.5 * (rlo + rhi);
+    for (int x = 0; x < S; x++) tabs[x] = static_cast<float>(f0[x] + 0.5 * c);
+    double rmax = 0;
+    for (int y = 0; y < S; y++)
+        for (int x = 0; x < S; x++) {
+            const double r = static_cast<double>(lmn[S + y * S + x]) - tabs[x] - tabs[y];
+            tabs[S + y * S + x] = static_cast<float>(r);
+            rmax = std::max(rmax, std::fabs(r));
+        }
+    return rmax;
+}
+
+// max |w| over the gridded samples and max |k| over the channels
+void w_k_max(const std::vector<p9idg_subgrid> &subs, const std::vector<double> &wn, const double *uvw_host,
+             int nt_all, double &wmax, double &kmax) {
+    wmax = 0;
+    kmax = 0;
+    for (double k : wn) kmax = std::max(kmax, std::fabs(k));
+    for (const auto &sg : subs)
+        for (int t = 0; t < sg.time_sample_count; t++) {
+            const double w = uvw_host[(static_cast<int64_t>(sg.baseline_idx) * nt_all + sg.time_sample_start + t) * 3 + 2];
+            wmax = std::max(wmax, std::fabs(w));
+        }
+}
+
+}  // namespace
+
+double tc_w_term(const std::vector<p9idg_subgrid> &subs, const std::vector<float> &lmn, int S,
+                 const std::vector<double> &wn, const double *uvw_host, int nt_all) {
+    if (S != kS) return INFINITY;
+    std::vector<float> tabs;
+    const double rmax = separable_tables(lmn, S, tabs);
+    double wmax, kmax;
+    w_k_max(subs, wn, uvw_host, nt_all, wmax, kmax);
+    return wmax * kmax * rmax;
+}
+
 p9idg_status tc_prepare(TcPlanState &st, const std::vector<p9idg_subgrid> &subs, const std::vector<float> &lmn,
                         int S, int nch, const std::vector<double> &wn, const double *uvw_host, int nt_all,
                         cudaStream_t stream, std::string &err) {
@@ -911,31 +977,16 @@ p9idg_status tc_prepare(TcPlanState &st, const std::vector<p9idg_subgrid> &subs,
         err = "tensor-core kernels support subgrid size 32 only";
         return P9IDG_UNSUPPORTED;
     }
-    // separable part of n and the remainder r (Gridder.cs:168-174 values in the lmn table)
-    std::vector<float> tabs(S + S * S);
-    for (int x = 0; x < S; x++) {
-        const double l = lmn[x], t = l * l;
-        tabs[x] = static_cast<float>(t / (t + std::sqrt(1.0 - t)));
-    }
-    double rmax = 0;
-    for (int y = 0; y < S; y++)
-        for (int x = 0; x < S; x++) {
-            const double r = static_cast<double>(lmn[S + y * S + x]) - tabs[x] - tabs[y];
-            tabs[S + y * S + x] = static_cast<float>(r);
-            rmax = std::max(rmax, std::fabs(r));
-        }
+    std::vector<float> tabs;
+    const double rmax = separable_tables(lmn, S, tabs);
     // coefficient offsets per subgrid and the largest |dw|
     std::vector<int64_t> off(subs.size() + 1, 0);
-    double wmax = 0, kmax = 0;
-    for (double k : wn) kmax = std::max(kmax, std::fabs(k));
-    for (size_t i = 0; i < subs.size(); i++) {
+    for (size_t i = 0; i < subs.size(); i++)
         off[i + 1] = off[i] + static_cast<int64_t>(subs[i].time_sample_count) * nch;
-        for (int t = 0; t < subs[i].time_sample_count; t++) {
-            const double w = uvw_host[(static_cast<int64_t>(subs[i].baseline_idx) * nt_all + subs[i].time_sample_start + t) * 3 + 2];
-            wmax = std::max(wmax, std::fabs(w));
-        }
-    }
+    double wmax, kmax;
+    w_k_max(subs, wn, uvw_host, nt_all, wmax, kmax);
     st.max_w_r = wmax * kmax * rmax;
+    st.dw_limit = rmax > 0 ? P9IDG_TC_MAX_W_TERM / rmax : INFINITY;
     for (int i = 0; i < S; i++) {
         st.m_tab[i] = lmn[i];
         st.g_tab[i] = tabs[i];
@@ -949,9 +1000,9 @@ p9idg_status tc_prepare(TcPlanState &st, const std::vector<p9idg_subgrid> &subs,
     };
     st.dw_scale = pow2_below(wmax * kmax * 1.0001);
     st.r_scale = pow2_below(rmax);
-    if (st.max_w_r > 0.05) {
+    if (!(st.max_w_r <= P9IDG_TC_MAX_W_TERM)) {
         err = "w term too large for the first-order separable tensor-core form (|dw r| = " +
-              std::to_string(st.max_w_r) + ")";
+              std::to_string(st.max_w_r) + " > " + std::to_string(P9IDG_TC_MAX_W_TERM) + ")";
         return P9IDG_UNSUPPORTED;
     }
     // degridder work items: whole time samples, up to degrid_chunk visibilities each
@@ -990,7 +1041,8 @@ static p9idg_status launch_coef(TcPlanState &st, const GridderArgs &a, int32_t n
                                 std::string &err) {
     if (nsub == 0 || st.coef_valid) return P9IDG_OK;
     tc_coef_kernel<<<nsub, 256, 0, stream>>>(a.subs, static_cast<const int64_t *>(st.coef_off), a.uvw, a.wavenumbers,
-                                             a.g, static_cast<float4 *>(st.coef), st.coef_recompute_flag);
+                                             a.g, static_cast<float4 *>(st.coef), st.coef_recompute_flag,
+                                             st.dw_limit, a.status);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
         err = std::string("coefficient kernel: ") + cudaGetErrorString(e);

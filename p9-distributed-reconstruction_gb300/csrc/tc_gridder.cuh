@@ -24,7 +24,8 @@ struct TcPlanState {
     int32_t nditems = 0;
     std::vector<WorkItem> ditems_host;  // the same list on the host (batches merge them)
     int64_t degrid_chunk = 8192;        // visibilities per degridder work item (set before tc_prepare)
-    double max_w_r = 0;           // max |dw| * max |r|: size of the neglected second-order term
+    double max_w_r = 0;           // max |dw| * max |r|: bound on the phase the first-order form expands
+    double dw_limit = 0;          // P9IDG_TC_MAX_W_TERM / max |r|: the largest |dw| a visibility may have
     float dw_scale = 1.f;         // FP16 mode: power of two with max |dw| * dw_scale < 1
     float r_scale = 1.f;          // FP16 mode: power of two with max |r| * r_scale < 1
     float m_tab[32] = {}, g_tab[32] = {};  // m_y and g_y (the same values serve l_x and f_x)
@@ -55,6 +56,11 @@ struct TcArgs {
 };
 
 bool tc_subgrid_size_supported(int S);
+// max |dw| * max |r| over the gridded samples of a plan: the largest phase dw * r(x, y) the
+// tensor-core form expands to first order (|dw| <= max |k| * max |w|, as WStepLambda is 0).
+// Host only; compared with P9IDG_TC_MAX_W_TERM before a plan selects a tensor-core mode.
+double tc_w_term(const std::vector<p9idg_subgrid> &subs, const std::vector<float> &lmn, int S,
+                 const std::vector<double> &wn, const double *uvw_host, int nt_all);
 // Per-problem arguments of a prepared plan (host side; device pointers inside).
 void tc_fill_args(const TcPlanState &st, const GridderArgs &a, TcArgs &t);
 // Coefficients for the plan's current uvw (no-op when still valid).

@@ -171,8 +171,12 @@ class Plan:
         _check(nat.lib().p9idg_plan_get_info(self.handle, ctypes.byref(i)))
         return {k: getattr(i, k) for k, _ in nat.PlanInfo._fields_}
 
-    def set_mode(self, mode: int):
+    def set_mode(self, mode: int) -> int:
+        """Selects the kernels; returns the mode the plan runs.  A tensor-core mode on a plan whose
+        w term exceeds TC_MAX_W_TERM keeps the FP32 kernels (``info()["tc_w_term"]`` says by how
+        much)."""
         _check(nat.lib().p9idg_plan_set_mode(self.handle, int(mode)))
+        return self.info()["mode"]
 
     def set_taper(self, taper):
         t = None if taper is None else np.ascontiguousarray(taper, np.float32)

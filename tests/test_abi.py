@@ -24,6 +24,13 @@ def test_header_declares_the_bound_surface():
     assert set(names) == set(pkg._native.SIGNATURES), set(names) ^ set(pkg._native.SIGNATURES)
 
 
+def test_integration_binds_every_declared_symbol():
+    """The P/Invoke declarations a C# maintainer adds cover the whole header."""
+    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    bound = set(re.findall(r"\bextern\s+\w+\s+(p9idg_[a-z0-9_]+)\s*\(", text))
+    assert bound == set(declared_functions()), set(declared_functions()) ^ bound
+
+
 def test_library_exports_every_declared_symbol():
     lib = ctypes.CDLL(pkg._native.LIB_PATH)
     missing = [n for n in declared_functions() if not hasattr(lib, n)]

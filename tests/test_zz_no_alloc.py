@@ -18,16 +18,17 @@ pytestmark = pytest.mark.gpu
 TOL = 1e-5
 
 
-def test_noalloc_matches_regular_entry_point(need_gpu):
+def _compare_two_calls(cd_over, min_subgrids=0):
     torch = pytest.importorskip("torch")
-    obs, cd = workload("meerkat_3072", n_ant=10, nt=300, nch=16)
-    c, cd = constants(cd)
+    obs, cd = workload("meerkat_3072", n_ant=10, nt=300 if not min_subgrids else 1000, nch=16)
+    c, cd = constants(cd, **cd_over)
     part = pkg.Partitioner.CreatePartition(c, obs.uvw, obs.frequencies)
     plan = part.plan
     stream = torch.cuda.current_stream()
     plan.set_stream(stream.cuda_stream)
     N, W = cd["grid_size"], cd["wlayer_count"]
     subs = plan.subgrids()
+    assert len(subs) >= max(1, min_subgrids)
     d_subs = torch.from_numpy(subs.view(np.int32).reshape(-1, 6).copy()).cuda()
     d_uvw = torch.from_numpy(obs.uvw).cuda()
     freq = np.ascontiguousarray(obs.frequencies, np.float64)
@@ -49,6 +50,18 @@ def test_noalloc_matches_regular_entry_point(need_gpu):
         assert st == 0, pkg._native.last_error()
         assert rel_l2(out.cpu().numpy(), ref.cpu().numpy()) < TOL
     plan.set_stream(0)
+
+
+@pytest.mark.parametrize("S,kernel", [(32, 8), (16, 4), (48, 8)])
+def test_noalloc_matches_regular_entry_point(need_gpu, S, kernel):
+    _compare_two_calls(dict(subgrid_size=S, kernel_size=kernel))
+
+
+def test_noalloc_several_batches(need_gpu):
+    """More subgrids than the scratch array holds at once (1,816 at S = 48): the call grids
+    them in consecutive batches that reuse the same descriptors, partial subgrids and status
+    word, and must still match the regular entry point."""
+    _compare_two_calls(dict(subgrid_size=48, kernel_size=8, max_timesteps=8), min_subgrids=2 * 1816 + 1)
 
 
 def test_noalloc_rejects_sizes_beyond_its_limits(need_gpu):
