@@ -349,6 +349,8 @@ typedef struct p9idg_mc_cycle {
     double image_ms;   /* WStackIFFTFloat + Shift + the gradient correlation */
     double deconv_ms;  /* GetAbsMaxDiff + Deconvolve */
     double degrid_ms;  /* model FFT + IDG.DeGridW + Visibilities.Substract */
+    double objective;  /* Residuals.CalcPenalty(dirty) + ElasticNet.CalcPenalty(x, lambdaTrue, alpha) before
+                          this cycle's deconvolution (MajorCycle.cs:102) */
 } p9idg_mc_cycle;
 /* Host arrays: vis complex128[nbl][nt][nch] (data.Visibilities), flags 1 byte per sample;
  * model_out (xImage) and residual_out (the last cycle's dirty image) float[N][N]; psf_out may be
@@ -413,6 +415,17 @@ p9idg_status p9idg_measure_sincos_peak(double *sincos_per_s, double *fma_per_s);
  * descriptors and TMEM path the P9IDG_MODE_TC_* kernels use; *max_rel_err is the largest error
  * relative to max |C| (inputs are exactly representable, so it is at FP32-accumulation level). */
 p9idg_status p9idg_tc_selftest(int32_t mode, int32_t n, double *max_rel_err);
+/* Fault injection for callers' error-path tests (no counterpart in the reference): after
+ * `after` more successful device allocations, every device allocation the library makes for its
+ * plans, deconvolvers and tensor-core state fails as cudaMalloc does when memory runs out, so the
+ * calls return P9IDG_OUT_OF_MEMORY; after < 0 turns it off.  Process-wide. */
+p9idg_status p9idg_debug_fail_device_allocations(int64_t after);
+/* Fault injection for the tensor-core kernels' bounded waits (no counterpart in the reference):
+ * later single-plan launches wait at most wait_ns per pipeline wait (0 = the default 2 s) and, if
+ * skip_stage >= 0, their loader warp never delivers input stage skip_stage of a work item, so the
+ * waits for it run out: the kernel frees its tensor memory once its issued MMAs have finished
+ * and the call returns P9IDG_DEVICE_CHECK_FAILED.  (0, -1) restores normal operation.  Process-wide. */
+p9idg_status p9idg_debug_tc_wait(int64_t wait_ns, int32_t skip_stage);
 
 #ifdef __cplusplus
 }

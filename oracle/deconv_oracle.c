@@ -362,6 +362,7 @@ int ocd_deconvolve(float *x, float *g, const float *a, int n, const float *psf2,
 typedef struct {
     float max_dirty, max_b, current_lambda, abs_max;
     int32_t deconvolved, converged, iterations, pad;
+    double objective; /* MajorCycle.cs:102, before this cycle's Deconvolve */
 } ocd_cycle;
 
 /* MajorCycle.ReconstructSerialCD (MajorCycle.cs:33-134) with the CPU deconvolver (FastSerialCD,
@@ -434,6 +435,8 @@ int ocd_major_cycle(const ocd_gparams *c, const ocd_gsubgrid *subs, int64_t nsub
         double lm = (l1 != l2) ? (!isnan(l1) ? (l2 < l1 ? l1 : l2) : l1) : (signbit(l2) ? l1 : l2);
         float current_lambda = (float)lm;
         float abs_max = ocd_get_abs_max_diff(model, grad, amap, N, lambda_true, alpha);
+        /* objective = Residuals.CalcPenalty(dirtyImage) + ElasticNet.CalcPenalty(xImage, lambdaTrue, alpha) */
+        rec->objective = ocd_residual_penalty(residual, nn) + ocd_elastic_net_penalty(model, N, N, lambda_true, alpha);
         rec->max_dirty = max_dirty;
         rec->max_b = max_b;
         rec->current_lambda = current_lambda;

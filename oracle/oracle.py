@@ -335,7 +335,8 @@ def set_num_threads(n):
 INDEX_OUT_OF_RANGE = 10
 
 CYCLE_DTYPE = np.dtype([("max_dirty", "<f4"), ("max_b", "<f4"), ("current_lambda", "<f4"), ("abs_max", "<f4"),
-                        ("deconvolved", "<i4"), ("converged", "<i4"), ("iterations", "<i4"), ("pad", "<i4")])
+                        ("deconvolved", "<i4"), ("converged", "<i4"), ("iterations", "<i4"), ("pad", "<i4"),
+                        ("objective", "<f8")])
 
 
 def _f32(a):

@@ -90,6 +90,8 @@ SIGNATURES = {
     "p9idg_grid_w_device_noalloc": (i32, [P, P, i64, P, i32, i32, P, i32, P, P, P]),
     "p9idg_plan_enable_timing": (i32, [P, i32]),
     "p9idg_plan_stage_times": (i32, [P, P, P]),
+    "p9idg_debug_fail_device_allocations": (i32, [i64]),
+    "p9idg_debug_tc_wait": (i32, [i64, i32]),
     "p9idg_plan_reset_timing": (i32, [P]),
     "p9idg_last_error": (ctypes.c_char_p, []),
     "p9idg_version": (ctypes.c_char_p, []),

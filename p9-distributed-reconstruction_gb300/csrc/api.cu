@@ -9,6 +9,7 @@
 #include <cufft.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -56,7 +57,7 @@ struct DevBuf {
         if (p) cudaFree(p);
         p = nullptr;
         bytes = 0;
-        cudaError_t e = cudaMalloc(&p, std::max<size_t>(n, 256));
+        cudaError_t e = device_alloc(&p, std::max<size_t>(n, 256));
         if (e == cudaSuccess) bytes = std::max<size_t>(n, 256);
         return e;
     }
@@ -108,6 +109,34 @@ struct PendingTiming {
 }  // namespace
 
 void p9idg::record_last_error(const std::string &msg) { g_last_error = msg; }
+
+namespace {
+// successful device allocations left before device_alloc fails (-1: never)
+std::atomic<int64_t> g_alloc_budget{-1};
+}  // namespace
+
+cudaError_t p9idg::device_alloc(void **p, size_t bytes) {
+    int64_t b = g_alloc_budget.load();
+    while (b >= 0) {
+        if (b == 0) {
+            *p = nullptr;
+            return cudaErrorMemoryAllocation;
+        }
+        if (g_alloc_budget.compare_exchange_weak(b, b - 1)) break;
+    }
+    return cudaMalloc(p, bytes);
+}
+
+extern "C" p9idg_status p9idg_debug_tc_wait(int64_t wait_ns, int32_t skip_stage) {
+    if (wait_ns < 0) return fail(P9IDG_INVALID_ARGUMENT, "negative wait limit");
+    tc_debug_set(static_cast<uint64_t>(wait_ns), skip_stage);
+    return P9IDG_OK;
+}
+
+extern "C" p9idg_status p9idg_debug_fail_device_allocations(int64_t after) {
+    g_alloc_budget.store(after < 0 ? -1 : after);
+    return P9IDG_OK;
+}
 
 struct p9idg_plan {
     p9idg_params c{};
@@ -290,12 +319,14 @@ p9idg_status ensure_device(p9idg_plan *p) {
     cudaError_t e = cudaGetDeviceCount(&count);
     if (e != cudaSuccess || count == 0) return fail(P9IDG_NO_DEVICE, "no CUDA device available");
     CK(cudaGetDevice(&p->device));
-    CK(cudaStreamCreateWithFlags(&p->own_stream, cudaStreamNonBlocking));
+    // each object is made once: a call that failed part-way (e.g. out of memory) and is retried
+    // continues from what exists
+    if (!p->own_stream) CK(cudaStreamCreateWithFlags(&p->own_stream, cudaStreamNonBlocking));
     if (!p->stream) p->stream = p->own_stream;
-    CK(cudaStreamCreateWithFlags(&p->side, cudaStreamNonBlocking));
-    CK(cudaEventCreateWithFlags(&p->ev_fork, cudaEventDisableTiming));
-    CK(cudaEventCreateWithFlags(&p->ev_join, cudaEventDisableTiming));
-    CK(cudaEventCreateWithFlags(&p->ev_mid, cudaEventDisableTiming));
+    if (!p->side) CK(cudaStreamCreateWithFlags(&p->side, cudaStreamNonBlocking));
+    if (!p->ev_fork) CK(cudaEventCreateWithFlags(&p->ev_fork, cudaEventDisableTiming));
+    if (!p->ev_join) CK(cudaEventCreateWithFlags(&p->ev_join, cudaEventDisableTiming));
+    if (!p->ev_mid) CK(cudaEventCreateWithFlags(&p->ev_mid, cudaEventDisableTiming));
     {
         int pageable = 0, host_tables = 0;
         CK(cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, p->device));
@@ -1183,9 +1214,9 @@ p9idg_status p9idg_plan_init_device(p9idg_plan *plan) {
 
 void p9idg_plan_destroy(p9idg_plan *plan) {
     if (!plan) return;
-    if (plan->dev_ready) {
+    if (plan->device >= 0) {  // device state exists (complete, or left part-way by a failed call)
         cudaSetDevice(plan->device);
-        cudaStreamSynchronize(plan->stream);
+        if (plan->stream) cudaStreamSynchronize(plan->stream);
         for (auto &pt : plan->pending) {
             cudaEventDestroy(pt.a);
             cudaEventDestroy(pt.b);

@@ -80,7 +80,7 @@ struct Buf {  // device buffer, freed when it goes out of scope (every early ret
         if (p) cudaFree(p);
         p = nullptr;
         bytes = 0;
-        cudaError_t e = cudaMalloc(&p, std::max<size_t>(n, 256));
+        cudaError_t e = device_alloc(&p, std::max<size_t>(n, 256));
         if (e == cudaSuccess) bytes = std::max<size_t>(n, 256);
         return e;
     }
@@ -486,6 +486,41 @@ __global__ void sumsq_kernel(const float *psf, int64_t count, double *partial) {
     }
 }
 
+// The two sums of the major cycle's objective (MajorCycle.cs:102) in the reference's types:
+// Residuals.CalcPenalty's float squares (Common.cs:253-260) and ElasticNet.CalcPenalty's
+// lambda * ElasticNetPenalty (Common.cs:22-23, 31-41; a float expression widened to double),
+// each summed in double: per-block partials, summed in block order on the host.
+__global__ void objective_kernel(const float *dirty, const float *x, int64_t count, float lambda, float alpha,
+                                 double *partial) {
+    __shared__ double sm[2][kWarps];
+    double sr = 0.0, sx = 0.0;
+    const float half_1ma = __fmul_rn(1.0f / 2.0f, __fsub_rn(1.0f, alpha));
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < count;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const float r = dirty[i], v = x[i];
+        sr = __dadd_rn(sr, static_cast<double>(__fmul_rn(r, r)));
+        const float pen = __fadd_rn(__fmul_rn(half_1ma, __fmul_rn(v, v)), __fmul_rn(alpha, fabsf(v)));
+        sx = __dadd_rn(sx, __dmul_rn(static_cast<double>(lambda), static_cast<double>(pen)));
+    }
+    for (int o = 16; o; o >>= 1) {
+        sr = __dadd_rn(sr, __shfl_xor_sync(0xffffffffu, sr, o));
+        sx = __dadd_rn(sx, __shfl_xor_sync(0xffffffffu, sx, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        sm[0][threadIdx.x >> 5] = sr;
+        sm[1][threadIdx.x >> 5] = sx;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int k = 1; k < kWarps; k++) {
+            sr = __dadd_rn(sr, sm[0][k]);
+            sx = __dadd_rn(sx, sm[1][k]);
+        }
+        partial[2 * blockIdx.x] = sr;
+        partial[2 * blockIdx.x + 1] = sx;
+    }
+}
+
 // PSF.Cut (Common.cs:216-226) of a square n x n image.
 __global__ void cut_kernel(const float *psf, int n, int m, int off, float *out) {
     const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
@@ -610,6 +645,25 @@ p9idg_status dev_max(const float *d_img, int n, int cut_factor, unsigned int *d_
     CK(cudaMemcpyAsync(&bits, d_word, sizeof(bits), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     std::memcpy(out, &bits, sizeof(float));
+    return P9IDG_OK;
+}
+
+// Residuals.CalcPenalty(dirty) + ElasticNet.CalcPenalty(x, lambda, alpha) (MajorCycle.cs:102).
+p9idg_status dev_objective(const float *d_dirty, const float *d_x, int64_t count, float lambda, float alpha,
+                           Buf &partial, double *out, cudaStream_t st) {
+    constexpr int kBlocks = 256;
+    CK(partial.ensure(sizeof(double) * 2 * kBlocks));
+    objective_kernel<<<kBlocks, kNT, 0, st>>>(d_dirty, d_x, count, lambda, alpha, partial.as<double>());
+    CK(cudaGetLastError());
+    double h[2 * kBlocks];
+    CK(cudaMemcpyAsync(h, partial.p, sizeof(h), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    double r = 0.0, x = 0.0;
+    for (int b = 0; b < kBlocks; b++) {
+        r += h[2 * b];
+        x += h[2 * b + 1];
+    }
+    *out = 0.5 * r + x;
     return P9IDG_OK;
 }
 
@@ -1383,6 +1437,7 @@ p9idg_status major_cycle(p9idg_plan *plan, const p9idg_mc_params *mp, const floa
         const float current_lambda = static_cast<float>(lm);
         float abs_max = 0.0f;
         TRY(p9idg_cd_get_abs_max_diff_device(cd, d_model, s.grad.as<float>(), lambda_true, mp->alpha, &abs_max));
+        TRY(dev_objective(d_residual, d_model, nn, lambda_true, mp->alpha, s.partial, &rec.objective, st));
         rec.max_dirty = max_dirty;
         rec.max_b = max_b;
         rec.current_lambda = current_lambda;

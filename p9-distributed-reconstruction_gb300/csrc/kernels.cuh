@@ -12,6 +12,11 @@ namespace p9idg {
 // uvw was checked when the mode was selected; this catches a different uvw passed to a call)
 enum : int32_t { kStatusIndex = 1, kStatusWait = 2, kStatusWTerm = 4 };
 
+// cudaMalloc for every device buffer the library keeps (plans, deconvolvers, tensor-core state),
+// failing with cudaErrorMemoryAllocation once p9idg_debug_fail_device_allocations has armed it
+// (api.cu).  The allocation-free entry point's fixed scratch array does not come through here.
+cudaError_t device_alloc(void **p, size_t bytes);
+
 // FFT.Shift (FFT.cs:221-264) as an index map on a square [n][n] array: the quadrant swap
 // of the leading 2*(n/2) rows/columns; for odd n the last row and column stay in place.
 __host__ __device__ inline void shift_index(int n, int &r, int &c) {

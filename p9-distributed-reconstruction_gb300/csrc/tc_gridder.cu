@@ -38,6 +38,7 @@
 #include <cuda_fp16.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 
@@ -99,11 +100,28 @@ struct Half16<false> {
     }
 };
 
-// (a, b) -> packed hi pair and packed lo pair (residuals)
-template <bool BF16>
+// (a, b) -> packed hi pair and packed lo pair (residuals).  MIXED: the residual x - hi is one
+// mixed-precision FMA per value (16-bit hi times -1 plus the FP32 x; exact, as hi is x rounded);
+// otherwise hi is widened back to FP32 and subtracted.  Both give the same bits; which is faster
+// was measured per kernel and type (the gridder: mixed for both types, 1.5 % on BF16; the
+// degridder: mixed for FP16, 2.4 % faster, the widening form for BF16, 7 % faster).
+template <bool BF16, bool MIXED = true>
 __device__ __forceinline__ void split_pair(float a, float b, uint32_t &hi, uint32_t &lo) {
     hi = Half16<BF16>::pack(a, b);
-    lo = Half16<BF16>::pack(a - Half16<BF16>::lo_of(hi), b - Half16<BF16>::hi_of(hi));
+    if (!MIXED) {
+        lo = Half16<BF16>::pack(a - Half16<BF16>::lo_of(hi), b - Half16<BF16>::hi_of(hi));
+        return;
+    }
+    float ra, rb;
+    if (BF16)
+        asm("{.reg .b16 h0, h1, m1;\n\tmov.b32 {h0, h1}, %2;\n\tmov.b16 m1, 0xBF80;\n\t"
+            "fma.rn.f32.bf16 %0, h0, m1, %3;\n\tfma.rn.f32.bf16 %1, h1, m1, %4;\n\t}"
+            : "=f"(ra), "=f"(rb) : "r"(hi), "f"(a), "f"(b));
+    else
+        asm("{.reg .b16 h0, h1, m1;\n\tmov.b32 {h0, h1}, %2;\n\tmov.b16 m1, 0xBC00;\n\t"
+            "fma.rn.f32.f16 %0, h0, m1, %3;\n\tfma.rn.f32.f16 %1, h1, m1, %4;\n\t}"
+            : "=f"(ra), "=f"(rb) : "r"(hi), "f"(a), "f"(b));
+    lo = Half16<BF16>::pack(ra, rb);
 }
 
 // The "memory" clobber keeps global loads from moving across these stores, so the kernels
@@ -271,7 +289,7 @@ __global__ void __launch_bounds__(kGThreads, 2)
             for (int i = 0; i < nstages; i++) {
                 const int s = i % kGStages;
                 const uint32_t ph = (i / kGStages) & 1;
-                if (!mbar_wait(&full[s], ph, abort_flag, kWaitNs)) {
+                if (!mbar_wait(&full[s], ph, abort_flag, a.wait_ns)) {
                     *abort_flag = 1;
                     atomicOr(a.status, kStatusWait);
                     break;
@@ -287,34 +305,61 @@ __global__ void __launch_bounds__(kGThreads, 2)
                 mma_commit(&empty[s]);
             }
             mma_commit(accb);
-            // the MMAs must be finished before the TMEM is released
-            if (!mbar_wait(accb, 0, abort_flag, kWaitNs)) atomicOr(a.status, kStatusWait);
+            // the MMAs must be finished before the TMEM is released: this wait does not stop early
+            // when another warp has aborted (only at its time limit)
+            volatile int never = 0;
+            if (!mbar_wait(accb, 0, &never, a.wait_ns)) atomicOr(a.status, kStatusWait);
         }
         __syncwarp();
     } else if (warp == kGLoaderWarp && TMA) {
         // ---- loader (TMA): stage i's 64 coefficients (one 2-D tile) and 66 visibilities from the
         // even index at or below the stage's first (one 1-D tile) -> ring slot i % kGRing
-        if (lane == 0) {
-            int issued = 0;
-            for (int i = 0; i < nstages; i++) {
-                const int slot = i % kGRing;
-                const uint32_t ph = (i / kGRing) & 1;
-                if (!mbar_wait(&in_empty[slot], ph ^ 1, abort_flag, kWaitNs)) {
+        // The last stage of an item, when it ends inside the stage, gets its visibilities from plain
+        // loads with the samples past the item's end written as zeros (a TMA tile would bring the
+        // next item's samples), so the producers never mask.
+        int issued = 0;
+        for (int i = 0; i < nstages; i++) {
+            const int slot = i % kGRing;
+            const uint32_t ph = (i / kGRing) & 1;
+            if (!warp_wait(&in_empty[slot], ph ^ 1, abort_flag, a.wait_ns)) {
+                if (lane == 0) {
                     *abort_flag = 1;
                     atomicOr(a.status, kStatusWait);
-                    break;
                 }
-                const uint32_t dst = rbase + slot * kGRingSlot;
-                mbar_expect_tx(&in_full[slot], kGVps * 16 + kVisBox * 8);
-                tma_load_2d(dst, &maps.coef, 0, static_cast<int32_t>(c0 + i * kGVps), &in_full[slot]);
-                tma_load_1d(dst + kGRingVis, &maps.vis, static_cast<int32_t>((v0 + i * kGVps) & ~int64_t(1)),
-                            &in_full[slot]);
-                issued = i + 1;
+                break;
             }
-            // tiles still in flight land before the CTA can exit (consumed ones have completed)
+            if (i == a.debug_skip_stage) {  // fault injection: this stage never arrives
+                issued = i + 1;
+                continue;
+            }
+            const uint32_t dst = rbase + slot * kGRingSlot;
+            const int valid = nvis - i * kGVps;
+            if (valid < kGVps) {
+                const int off = static_cast<int>((v0 + i * kGVps) & 1);
+                float2 *rvw = reinterpret_cast<float2 *>(ring + slot * kGRingSlot + kGRingVis) + off;
+                const float2 *src = reinterpret_cast<const float2 *>(vrow) + i * kGVps;
+#pragma unroll
+                for (int h = 0; h < kGVps / 32; h++) {
+                    const int q = lane + 32 * h;
+                    rvw[q] = q < valid ? src[q] : make_float2(0.f, 0.f);
+                }
+                fence_proxy_async();  // later TMA copies into this slot are ordered after these stores
+                __syncwarp();
+            }
+            if (lane == 0) {
+                mbar_expect_tx(&in_full[slot], kGVps * 16 + (valid < kGVps ? 0 : kVisBox * 8));
+                tma_load_2d(dst, &maps.coef, 0, static_cast<int32_t>(c0 + i * kGVps), &in_full[slot]);
+                if (valid >= kGVps)
+                    tma_load_1d(dst + kGRingVis, &maps.vis, static_cast<int32_t>((v0 + i * kGVps) & ~int64_t(1)),
+                                &in_full[slot]);
+            }
+            issued = i + 1;
+        }
+        // tiles still in flight land before the CTA can exit (consumed ones have completed)
+        if (lane == 0) {
             volatile int never = 0;
             for (int i = issued > kGRing ? issued - kGRing : 0; i < issued; i++)
-                if (!mbar_wait(&in_full[i % kGRing], (i / kGRing) & 1, &never, kWaitNs)) atomicOr(a.status, kStatusWait);
+                if (!mbar_wait(&in_full[i % kGRing], (i / kGRing) & 1, &never, a.wait_ns)) atomicOr(a.status, kStatusWait);
         }
         __syncwarp();
     } else if (warp == kGLoaderWarp) {
@@ -322,13 +367,14 @@ __global__ void __launch_bounds__(kGThreads, 2)
         for (int i = 0; i < nstages; i++) {
             const int slot = i % kGRing;
             const uint32_t ph = (i / kGRing) & 1;
-            if (!warp_wait(&in_empty[slot], ph ^ 1, abort_flag, kWaitNs)) {
+            if (!warp_wait(&in_empty[slot], ph ^ 1, abort_flag, a.wait_ns)) {
                 if (lane == 0) {
                     *abort_flag = 1;
                     atomicOr(a.status, kStatusWait);
                 }
                 break;
             }
+            if (i == a.debug_skip_stage) continue;  // fault injection: this stage never arrives
             const uint32_t dst = rbase + slot * kGRingSlot;
 #pragma unroll
             for (int h = 0; h < kGVps / 32; h++) {
@@ -351,13 +397,6 @@ __global__ void __launch_bounds__(kGThreads, 2)
         const int yy = lane, kg = warp, kv = kg * 8;
         const float m_y = a.lmn[yy], g_y = a.tabs[yy];  // y-side tables (l and m coincide, f and g coincide)
         const float l_x = m_y, f_x = g_y;
-        float ep_r[4], ep_t[4];  // remainder r and taper of the 4 pixels this thread finishes
-#pragma unroll
-        for (int k = 0; k < 4; k++) {
-            const int p = threadIdx.x + k * kGProducerWarps * 32;
-            ep_r[k] = a.tabs[kS + p];
-            ep_t[k] = a.taper[p];
-        }
         float sv = 1.f;  // FP16: power-of-two scale of this item's visibilities
         if (!BF16) {
             float mx = 0.f;
@@ -371,7 +410,7 @@ __global__ void __launch_bounds__(kGThreads, 2)
         for (int i = 0; i < nstages; i++) {
             const int s = i % kGStages, slot = i % kGRing;
             const uint32_t ph = (i / kGStages) & 1, iph = (i / kGRing) & 1;
-            if (!warp_wait(&in_full[slot], iph, abort_flag, kWaitNs)) {
+            if (!warp_wait(&in_full[slot], iph, abort_flag, a.wait_ns)) {
                 if (lane == 0) {
                     *abort_flag = 1;
                     atomicOr(a.status, kStatusWait);
@@ -381,7 +420,7 @@ __global__ void __launch_bounds__(kGThreads, 2)
             // the ring slot is released only after the values read from it have been used (below):
             // an arrive right after the loads could let the next copy into the slot overtake a
             // shared-memory load still queued, which would then return the next stage's data
-            if (!warp_wait(&empty[s], ph ^ 1, abort_flag, kWaitNs)) {
+            if (!warp_wait(&empty[s], ph ^ 1, abort_flag, a.wait_ns)) {
                 if (lane == 0) {
                     *abort_flag = 1;
                     atomicOr(a.status, kStatusWait);
@@ -391,8 +430,6 @@ __global__ void __launch_bounds__(kGThreads, 2)
             const float4 *rc = reinterpret_cast<const float4 *>(ring + slot * kGRingSlot) + kv;
             const int off = TMA ? static_cast<int>((v0 + i * kGVps) & 1) : 0;
             const VisT *rv = reinterpret_cast<const VisT *>(ring + slot * kGRingSlot + kGRingVis) + off + kv;
-            // a TMA tile past the item's end holds the next item's samples: weight them 0
-            const int valid = TMA ? nvis - (i * kGVps + kv) : kGVps;
             // words: [pair][row] with row = Bh_re, Bh_im, B1_re, B1_im, Bl_re, Bl_im, Wh_re, Wh_im,
             // Wl_re, Wl_im; a pair packs visibilities (2p, 2p+1) of this warp's eight
             uint32_t wd[4][10];
@@ -403,8 +440,7 @@ __global__ void __launch_bounds__(kGThreads, 2)
                 for (int u = 0; u < 2; u++) {
                     const int v = 2 * pr + u;
                     const float4 c = rc[v];
-                    float2 vv = load_vis(rv, v);
-                    if (TMA && v >= valid) vv = make_float2(0.f, 0.f);
+                    const float2 vv = load_vis(rv, v);
                     // y side: B_k(y)
                     __sincosf(fmaf(c.y, m_y, c.z * g_y), &sb[u], &cb[u]);
                     dws[u] = c.z * sw;
@@ -443,7 +479,7 @@ __global__ void __launch_bounds__(kGThreads, 2)
             }
         }
         // ---- epilogue: TMEM -> smem planes -> partial subgrid
-        const bool ok = warp_wait(accb, 0, abort_flag, kWaitNs);
+        const bool ok = warp_wait(accb, 0, abort_flag, a.wait_ns);
         tc_fence_after();
         float *E = reinterpret_cast<float *>(smem);  // the stages are free once accb completed
         // warp: lane quarter q (rows (Bh+Bl)_re, (Bh+Bl)_im, B1_re, B1_im) against the real (h = 0)
@@ -465,6 +501,13 @@ __global__ void __launch_bounds__(kGThreads, 2)
         tc_fence_before();
         named_bar(1, kGProducerWarps * 32);
         if (ok && !*abort_flag) {
+            float ep_r[4], ep_t[4];  // remainder r and taper of the 4 pixels this thread finishes
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const int p = threadIdx.x + k * kGProducerWarps * 32;
+                ep_r[k] = a.tabs[kS + p];
+                ep_t[k] = a.taper[p];
+            }
             float2 *out = a.partials + static_cast<int64_t>(it.slot) * kS * kS;
             const float i0 = 1.f / sv, i1 = 1.f / (sv * sw);  // exact: powers of two
 #pragma unroll
@@ -609,6 +652,7 @@ __global__ void __launch_bounds__(kDThreads, 2)
     const uint32_t tmem = *tmem_slot;
     const uint32_t bs = smem_u32(bstat), ts = smem_u32(tiles), rbase = smem_u32(ring);
 
+    int drain_phase = 0;  // MMA warp: commits to a_empty[0] before the drain commit
     if (warp == kDMmaWarp) {
         // ---- MMA issuer
         if (lane == 0) {
@@ -616,8 +660,8 @@ __global__ void __launch_bounds__(kDThreads, 2)
             for (int i = 0; i < ntiles; i++) {
                 const int b = i & 1;
                 const uint32_t ph = (i >> 1) & 1;
-                if (!mbar_wait(&a_full[b], ph, abort_flag, kWaitNs) ||
-                    !mbar_wait(&acc_empty[b], ph ^ 1, abort_flag, kWaitNs)) {
+                if (!mbar_wait(&a_full[b], ph, abort_flag, a.wait_ns) ||
+                    !mbar_wait(&acc_empty[b], ph ^ 1, abort_flag, a.wait_ns)) {
                     *abort_flag = 1;
                     atomicOr(a.status, kStatusWait);
                     break;
@@ -635,6 +679,7 @@ __global__ void __launch_bounds__(kDThreads, 2)
                 }
                 mma_commit(&a_empty[b]);
                 mma_commit(&acc_full[b]);
+                if (b == 0) drain_phase++;
             }
             // drain: every issued MMA finished before the TMEM is released
             mma_commit(&a_empty[0]);
@@ -648,10 +693,14 @@ __global__ void __launch_bounds__(kDThreads, 2)
             for (int i = 0; i < ntiles; i++) {
                 const int slot = i % kDRing;
                 const uint32_t ph = (i / kDRing) & 1;
-                if (!mbar_wait(&in_empty[slot], ph ^ 1, abort_flag, kWaitNs)) {
+                if (!mbar_wait(&in_empty[slot], ph ^ 1, abort_flag, a.wait_ns)) {
                     *abort_flag = 1;
                     atomicOr(a.status, kStatusWait);
                     break;
+                }
+                if (i == a.debug_skip_stage) {  // fault injection: this tile never arrives
+                    issued = i + 1;
+                    continue;
                 }
                 mbar_expect_tx(&in_full[slot], kDTile * 16);
                 tma_load_2d(rbase + slot * kDRingSlot, &maps.coef, 0, static_cast<int32_t>(c0 + i * kDTile),
@@ -660,7 +709,7 @@ __global__ void __launch_bounds__(kDThreads, 2)
             }
             volatile int never = 0;
             for (int i = issued > kDRing ? issued - kDRing : 0; i < issued; i++)
-                if (!mbar_wait(&in_full[i % kDRing], (i / kDRing) & 1, &never, kWaitNs)) atomicOr(a.status, kStatusWait);
+                if (!mbar_wait(&in_full[i % kDRing], (i / kDRing) & 1, &never, a.wait_ns)) atomicOr(a.status, kStatusWait);
         }
         __syncwarp();
     } else if (warp == kDLoaderWarp) {
@@ -668,13 +717,14 @@ __global__ void __launch_bounds__(kDThreads, 2)
         for (int i = 0; i < ntiles; i++) {
             const int slot = i % kDRing;
             const uint32_t ph = (i / kDRing) & 1;
-            if (!warp_wait(&in_empty[slot], ph ^ 1, abort_flag, kWaitNs)) {
+            if (!warp_wait(&in_empty[slot], ph ^ 1, abort_flag, a.wait_ns)) {
                 if (lane == 0) {
                     *abort_flag = 1;
                     atomicOr(a.status, kStatusWait);
                 }
                 break;
             }
+            if (i == a.debug_skip_stage) continue;  // fault injection: this tile never arrives
             const uint32_t dst = rbase + slot * kDRingSlot;
 #pragma unroll
             for (int u = 0; u < 4; u++) {
@@ -699,7 +749,7 @@ __global__ void __launch_bounds__(kDThreads, 2)
         for (int i = 0; i < ntiles; i++) {
             const int b = i & 1, slot = i % kDRing;
             const uint32_t ph = (i >> 1) & 1, iph = (i / kDRing) & 1;
-            if (!warp_wait(&in_full[slot], iph, abort_flag, kWaitNs)) {
+            if (!warp_wait(&in_full[slot], iph, abort_flag, a.wait_ns)) {
                 if (lane == 0) {
                     *abort_flag = 1;
                     atomicOr(a.status, kStatusWait);
@@ -716,7 +766,7 @@ __global__ void __launch_bounds__(kDThreads, 2)
                 }
             }
             // the slot is released once cu has been used (below), not right after the loads
-            if (!warp_wait(&a_empty[b], ph ^ 1, abort_flag, kWaitNs)) {
+            if (!warp_wait(&a_empty[b], ph ^ 1, abort_flag, a.wait_ns)) {
                 if (lane == 0) {
                     *abort_flag = 1;
                     atomicOr(a.status, kStatusWait);
@@ -732,7 +782,7 @@ __global__ void __launch_bounds__(kDThreads, 2)
                 for (int v = 0; v < 4; v++) {
                     float sa, ca;
                     __sincosf(fmaf(cu[u].x, lx[v], cu[u].y * fx[v]), &sa, &ca);
-                    split_pair<BF16>(ca, sa, whi[v], wlo[v]);
+                    split_pair<BF16, !BF16>(ca, sa, whi[v], wlo[v]);
                 }
                 st_shared_v4(ahi + cc * 16, whi[0], whi[1], whi[2], whi[3]);
                 st_shared_v4(alo + cc * 16, wlo[0], wlo[1], wlo[2], wlo[3]);
@@ -752,7 +802,7 @@ __global__ void __launch_bounds__(kDThreads, 2)
             const int b = i & 1, slot = i % kDRing;
             const uint32_t ph = (i >> 1) & 1, iph = (i / kDRing) & 1;
             const int row = q * 32 + lane, j = i * kDTile + row;
-            if (!warp_wait(&in_full[slot], iph, abort_flag, kWaitNs)) {
+            if (!warp_wait(&in_full[slot], iph, abort_flag, a.wait_ns)) {
                 if (lane == 0) {
                     *abort_flag = 1;
                     atomicOr(a.status, kStatusWait);
@@ -761,7 +811,7 @@ __global__ void __launch_bounds__(kDThreads, 2)
             }
             const float4 c = reinterpret_cast<const float4 *>(ring + slot * kDRingSlot)[row];
             // the slot is released once c has been used (below), not right after the load
-            if (!warp_wait(&acc_full[b], ph, abort_flag, kWaitNs)) {
+            if (!warp_wait(&acc_full[b], ph, abort_flag, a.wait_ns)) {
                 if (lane == 0) {
                     *abort_flag = 1;
                     atomicOr(a.status, kStatusWait);
@@ -808,10 +858,12 @@ __global__ void __launch_bounds__(kDThreads, 2)
     tc_fence_before();
     __syncthreads();
     if (warp == kDMmaWarp) {
-        // wait (bounded) for the drain commit: all MMAs of this CTA are complete
+        // wait (bounded) for the drain commit: all MMAs of this CTA are complete.  The phase count
+        // is what was issued (fewer tiles after an abort), and the wait does not stop early on an
+        // abort: the TMEM may only be released once no MMA is in flight.
         if (lane == 0) {
-            const int nb0 = (ntiles + 1) / 2;  // completed phases of a_empty[0] before the drain
-            if (!mbar_wait(&a_empty[0], static_cast<uint32_t>(nb0 & 1), abort_flag, kWaitNs) && !*abort_flag)
+            volatile int never = 0;
+            if (!mbar_wait(&a_empty[0], static_cast<uint32_t>(drain_phase & 1), &never, a.wait_ns))
                 atomicOr(a.status, kStatusWait);
         }
         __syncwarp();
@@ -892,7 +944,12 @@ cudaError_t set_smem(K kernel, uint32_t bytes) {
     return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes));
 }
 
+std::atomic<uint64_t> g_wait_ns{kWaitNs};
+std::atomic<int32_t> g_skip_stage{-1};
+
 void fill_args(TcArgs &t, const GridderArgs &a, const TcPlanState &st) {
+    t.wait_ns = g_wait_ns.load();
+    t.debug_skip_stage = g_skip_stage.load();
     t.g = a.g;
     t.subs = a.subs;
     t.coef_off = static_cast<const int64_t *>(st.coef_off);
@@ -911,6 +968,11 @@ void fill_args(TcArgs &t, const GridderArgs &a, const TcPlanState &st) {
 }  // namespace
 
 bool tc_subgrid_size_supported(int S) { return S == kS; }
+
+void tc_debug_set(uint64_t wait_ns, int32_t skip_stage) {
+    g_wait_ns.store(wait_ns > 0 ? wait_ns : kWaitNs);
+    g_skip_stage.store(skip_stage);
+}
 
 namespace {
 
@@ -1011,10 +1073,10 @@ p9idg_status tc_prepare(TcPlanState &st, const std::vector<p9idg_subgrid> &subs,
     build_work_items(subs, nch, st.degrid_chunk, dtmp, ditems);
     st.ncoef = off.back();
     cudaError_t e;
-    if ((e = cudaMalloc(&st.coef, sizeof(float4) * std::max<int64_t>(1, st.ncoef))) != cudaSuccess ||
-        (e = cudaMalloc(&st.coef_off, sizeof(int64_t) * off.size())) != cudaSuccess ||
-        (e = cudaMalloc(&st.tables, sizeof(float) * tabs.size())) != cudaSuccess ||
-        (e = cudaMalloc(&st.ditems, sizeof(WorkItem) * std::max<size_t>(1, ditems.size()))) != cudaSuccess) {
+    if ((e = device_alloc(&st.coef, sizeof(float4) * std::max<int64_t>(1, st.ncoef))) != cudaSuccess ||
+        (e = device_alloc(&st.coef_off, sizeof(int64_t) * off.size())) != cudaSuccess ||
+        (e = device_alloc(&st.tables, sizeof(float) * tabs.size())) != cudaSuccess ||
+        (e = device_alloc(&st.ditems, sizeof(WorkItem) * std::max<size_t>(1, ditems.size()))) != cudaSuccess) {
         err = std::string("tensor-core buffers: ") + cudaGetErrorString(e);
         tc_release(st);
         return e == cudaErrorMemoryAllocation ? P9IDG_OUT_OF_MEMORY : P9IDG_CUDA_ERROR;

@@ -53,9 +53,14 @@ struct TcArgs {
     float m_tab[32], g_tab[32];
     int32_t *done;   // batched launches: completion count / time (see GridderArgs)
     unsigned long long *finish_ns;
+    uint64_t wait_ns;          // limit of every pipeline wait before the kernel gives up (2 s)
+    int32_t debug_skip_stage;  // fault injection: the loader never delivers this stage (-1: off)
 };
 
 bool tc_subgrid_size_supported(int S);
+// Fault injection for the bounded-wait path (p9idg_debug_tc_wait): later launches use this wait
+// limit and have their loader skip input stage `skip_stage` of every work item (-1: off).
+void tc_debug_set(uint64_t wait_ns, int32_t skip_stage);
 // max |dw| * max |r| over the gridded samples of a plan: the largest phase dw * r(x, y) the
 // tensor-core form expands to first order (|dw| <= max |k| * max |w|, as WStepLambda is 0).
 // Host only; compared with P9IDG_TC_MAX_W_TERM before a plan selects a tensor-core mode.

@@ -55,7 +55,8 @@ class McCycle(ctypes.Structure):
     _fields_ = [("max_dirty", ctypes.c_float), ("max_b", ctypes.c_float), ("current_lambda", ctypes.c_float),
                 ("abs_max", ctypes.c_float), ("deconvolved", ctypes.c_int32), ("converged", ctypes.c_int32),
                 ("iterations", ctypes.c_int32), ("reserved", ctypes.c_int32), ("grid_ms", ctypes.c_double),
-                ("image_ms", ctypes.c_double), ("deconv_ms", ctypes.c_double), ("degrid_ms", ctypes.c_double)]
+                ("image_ms", ctypes.c_double), ("deconv_ms", ctypes.c_double), ("degrid_ms", ctypes.c_double),
+                ("objective", ctypes.c_double)]
 
 
 def _f32(a, writable=False):

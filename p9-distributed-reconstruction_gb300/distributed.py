@@ -26,6 +26,40 @@ def baseline_block(nbl: int, world_size: int, rank: int) -> tuple[int, int]:
     return begin, end
 
 
+def balanced_baseline_blocks(weights, world_size: int) -> list[tuple[int, int]]:
+    """Contiguous [begin, end) baseline blocks, one per rank, with about equal total weight
+    (e.g. gridded visibilities per baseline; the partitioner drops samples unevenly, so equal
+    baseline counts would leave ranks with very different work).  Rank r's block ends at the
+    baseline boundary whose running weight is closest to (r + 1) / world_size of the total; every
+    block is contiguous, so each rank's partition is the global partition's subgrids of those
+    baselines, in order."""
+    w = np.asarray(weights, dtype=np.float64)
+    if world_size <= 0:
+        raise ValueError("invalid world size")
+    if np.any(w < 0):
+        raise ValueError("negative weight")
+    nbl = len(w)
+    cum = np.concatenate([[0.0], np.cumsum(w)])
+    total = cum[-1]
+    bounds = [0]
+    for r in range(1, world_size):
+        target = total * r / world_size
+        b = int(np.searchsorted(cum, target, side="left"))
+        if b > 0 and (b > nbl or target - cum[b - 1] <= cum[b] - target):
+            b -= 1
+        bounds.append(min(max(b, bounds[-1]), nbl))
+    bounds.append(nbl)
+    return [(bounds[r], bounds[r + 1]) for r in range(world_size)]
+
+
+def gridded_per_baseline(subgrids, nbl: int, nch: int) -> np.ndarray:
+    """Visibilities each baseline contributes to a plan's subgrids (time samples x channels)."""
+    out = np.zeros(nbl, np.int64)
+    np.add.at(out, np.asarray(subgrids["baseline_idx"], np.int64),
+              np.asarray(subgrids["time_sample_count"], np.int64) * nch)
+    return out
+
+
 def local_block(arrays, nbl, world_size, rank):
     """Slices this rank's baselines out of [nbl, ...] arrays (uvw, visibilities, flags)."""
     b, e = baseline_block(nbl, world_size, rank)
@@ -80,6 +114,29 @@ class GridReducer:
         """In-place all-reduce of a device tensor (complex64 grids are summed as float pairs)."""
         t = self.torch.view_as_real(tensor) if tensor.is_complex() else tensor
         self.dist.all_reduce(t, op=self.dist.ReduceOp.SUM, group=self.group)
+        return tensor
+
+    def sum_layers_device_(self, layers, root=None):
+        """Dirty-image form of the grid reduce: WStackIFFTFloat applies no per-layer w correction
+        (FFT.cs:188-215), so only the sum of the W layers matters.  Sums this rank's layers into
+        layer 0 on the device, then reduces that one N x N grid across ranks (N^2 * 8 bytes for
+        complex64, W times less than the layer stack): to every rank (root None) or to `root`.
+        Returns layer 0 (the summed grid on the ranks that receive it)."""
+        grid = layers[0]
+        for w in range(1, layers.shape[0]):
+            grid.add_(layers[w])
+        t = self.torch.view_as_real(grid) if grid.is_complex() else grid
+        if root is None:
+            self.dist.all_reduce(t, op=self.dist.ReduceOp.SUM, group=self.group)
+        else:
+            self.dist.reduce(t, dst=root, op=self.dist.ReduceOp.SUM, group=self.group)
+        return grid
+
+    def broadcast_device_(self, tensor, root: int = 0):
+        """In-place broadcast of a device (or, with gloo, host) tensor from `root`: the model grid
+        every rank degrids (MPIMajorCycle.cs:106)."""
+        t = self.torch.view_as_real(tensor) if tensor.is_complex() else tensor
+        self.dist.broadcast(t, src=root, group=self.group)
         return tensor
 
     def broadcast(self, arr, root: int = 0):
