@@ -401,6 +401,34 @@ def run_major_cycle(args):
                "residual_rel_l2_gpu_fp32_vs_cpu": rel(g["residual"], ref["residual"]),
                "model_rel_l2_gpu_tc_vs_cpu": rel(gt["model"], ref["model"]),
                "residual_rel_l2_gpu_tc_vs_cpu": rel(gt["residual"], ref["residual"])}
+        cpu["objective_per_cycle_cpu_gpu_fp32_gpu_tc"] = [
+            (float(r), float(x["objective"]), float(y["objective"]))
+            for r, x, y in zip(ref["cycles"]["objective"], g["cycles"], gt["cycles"])]
+    first = None
+    if args.mc_cpu_full and not args.no_cpu_baseline:
+        # the FP64 oracle on the full 3072^2 observation: PSF, first dirty image, gradients and the
+        # first CD decisions of the first major cycle, against the GPU loop run to the same point
+        oracle = load_oracle()
+        n_it = 200
+        subs = oracle.partition(cd, obs.uvw, obs.frequencies)
+        t0 = time.perf_counter()
+        ref = oracle.major_cycle(cd, subs, obs.uvw, obs.frequencies, obs.vis, obs.flags.astype(np.uint8),
+                                 kw["psfCutFactor"], 1, kw["lambda_"], kw["alpha"], n_it, kw["deconvEpsilon"])
+        cpu_full_s = time.perf_counter() - t0
+        part_kw = dict(kw, maxMajorCycle=1, deconvIterations=n_it)
+        first = {"cpu_s": cpu_full_s, "cd_iterations": n_it, "cores": oracle.num_threads()}
+        for m in ("fp32", "tc_bf16x3"):
+            gg = gpu_loop(obs, cd, m, part_kw)
+            same_px = np.array_equal(np.flatnonzero(gg["model"]), np.flatnonzero(ref["model"]))
+            first[m] = {"psf_rel_l2": rel(gg["psf"], ref["psf"]),
+                        "first_dirty_image_rel_l2": rel(gg["residual"], ref["residual"]),
+                        "max_b_gpu_cpu": (float(gg["cycles"][0]["max_b"]), float(ref["cycles"]["max_b"][0])),
+                        "objective_gpu_cpu": (float(gg["cycles"][0]["objective"]),
+                                              float(ref["cycles"]["objective"][0])),
+                        "model_rel_l2": rel(gg["model"], ref["model"]),
+                        "same_selected_pixels": bool(same_px),
+                        "nonzero_pixels_gpu_cpu": (int(np.count_nonzero(gg["model"])),
+                                                   int(np.count_nonzero(ref["model"])))}
     slim = [{k: (round(v, 4) if isinstance(v, float) else v) for k, v in c.items()} for c in tc["cycles"]]
     out = {"metric": f"s per {args.mc_cycles}-cycle serial-CD reconstruction at 3072^2 (BF16x3 gridder)",
            "value": tc["wall_s"], "unit": "s", "n_gpus": 1, "steps": 1, "warmup": 1,
@@ -416,6 +444,9 @@ def run_major_cycle(args):
            "model_rel_l2_tc_vs_fp32": rel(tc["model"], fp["model"]),
            "residual_rel_l2_tc_vs_fp32": rel(tc["residual"], fp["residual"]),
            "psf_rel_l2_tc_vs_fp32": rel(tc["psf"], fp["psf"]),
+           "objective_per_cycle_tc_fp32": [(float(x["objective"]), float(y["objective"]))
+                                           for x, y in zip(tc["cycles"], fp["cycles"])],
+           "first_cycle_vs_cpu_full_size": first,
            "cpu_baseline": cpu, "clocks": tc["clocks"]}
     print(json.dumps(out), flush=True)
     return 0
@@ -430,7 +461,7 @@ def run_batched(args):
     synth = entry._load_module(entry.PKG_NAME + ".synth", os.path.join(entry.PKG_DIR, "synth.py"))
     mode_name = "tc_bf16x3" if args.mode == "auto" else args.mode
     t0 = time.perf_counter()
-    geos = [synth.build_geometry(w) for w in synth.batched_workloads(args.batched, seed=4)]
+    geos = [synth.build_geometry(w) for w in synth.batched_workloads(args.batched, seed=4, mix=args.mix)]
     big = max(range(len(geos)), key=lambda i: geos[i][0].shape[0] * geos[i][0].shape[1] * len(geos[i][1]))
     uvw_b, f_b, cd_b = geos[big]
     tune = pkg.autotune(pkg.GriddingConstants.from_dict(cd_b), uvw_b, f_b, MODES[mode_name],
@@ -513,7 +544,10 @@ def run_batched(args):
            "value": value, "unit": "Mvis/s", "n_gpus": 1, "steps": args.steps, "warmup": max(3, args.warmup),
            "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
            "dtype": mode_name, "data": "synthetic geometry (seeded); random complex64 visibilities and model grids",
-           "config": {"workload": f"{len(geos)} problems: N 512-2048, 200-2000 times, 4-32 channels, 16-64 antennas",
+           "config": {"workload": (f"{len(geos)} problems: N 512-2048, 200-2000 times, 4-32 channels, 16-64 antennas"
+                                   if args.mix == "config" else
+                                   f"{len(geos)} small problems: N 512-1024, 200-500 times, 4-16 channels, "
+                                   f"16-32 antennas"),
                       "mode": mode_name, "tuning": tune, "gridded_visibilities": int(gridded),
                       "input_visibilities": int(sum(i["input_visibilities"] for i in info)),
                       "subgrids": int(sum(i["num_subgrids"] for i in info)), "setup_s": round(setup_s, 2),
@@ -585,10 +619,15 @@ def main():
                     help="smaller array (fewer baselines) of the same workload, for profiling captures")
     ap.add_argument("--batched", type=int, default=0,
                     help="instead: N independent problems of mixed sizes in one batch (graph-replayed)")
+    ap.add_argument("--mix", default="config", choices=["config", "small"],
+                    help="--batched problem mix: the configured sizes, or problems too small to fill the GPU")
     ap.add_argument("--major-cycle", action="store_true",
                     help="instead: the serial-CD major-cycle loop on the same workload")
     ap.add_argument("--mc-cycles", type=int, default=6)
     ap.add_argument("--mc-iterations", type=int, default=30000)
+    ap.add_argument("--mc-cpu-full", action="store_true",
+                    help="--major-cycle: also run the FP64 oracle's first cycle (PSF, dirty image, 200 CD "
+                         "iterations) on the full 3072^2 observation (about a minute of host cores)")
     ap.add_argument("--cd", type=int, default=0,
                     help="instead: this many FastSerialCD iterations at 3072^2 (iterations/s)")
     args = ap.parse_args()

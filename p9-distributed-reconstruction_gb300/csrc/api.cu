@@ -953,6 +953,12 @@ struct p9idg_batch {
     DevBuf d_gitems, d_ditems, d_refs, d_done_init, d_done, d_finish, d_start;
     int32_t ngitems = 0, nditems = 0, nrefs = 0;
     std::vector<WorkItem> h_gitems, h_ditems;  // merged work items of all problems, in launch order
+    // FP32 batches may mix subgrid sizes: the items and subgrid references are grouped by size,
+    // one launch per kernel stage and size (group k: items [g0, g0 + gn), [d0, d0 + dn), refs [r0, r0 + rn))
+    struct Group {
+        int32_t S, g0, gn, d0, dn, r0, rn;
+    };
+    std::vector<Group> groups;
     std::vector<int64_t> prob_vis;             // visibilities per problem (for the schedules)
     int32_t schedule = P9IDG_SCHEDULE_THROUGHPUT;
     std::vector<void *> layers, vis_out;
@@ -968,22 +974,25 @@ __global__ void stamp_kernel(unsigned long long *t) { *t = device_ns(); }
 p9idg_status batch_grid(p9idg_batch *b) {
     for (size_t i = 0; i < b->plans.size(); i++)
         CK(cudaMemsetAsync(b->layers[i], 0, b->layer_bytes[i], b->stream));
-    GridderArgs L{};
-    L.g.S = b->S;
-    L.items = b->d_gitems.as<WorkItem>();
-    L.nitems = b->ngitems;
-    if (b->mode == P9IDG_MODE_FP32) {
-        CK(launch_gridder_fp32(L, b->stream, b->d_gargs.as<GridderArgs>()));
-    } else {
-        TRY(tc_grid_batch(b->d_tg.as<TcArgs>(), b->d_gitems.as<WorkItem>(), b->ngitems, b->mode, b->stream,
-                          g_last_error));
+    for (const auto &g : b->groups) {
+        GridderArgs L{};
+        L.g.S = g.S;
+        L.items = b->d_gitems.as<WorkItem>() + g.g0;
+        L.nitems = g.gn;
+        if (b->mode == P9IDG_MODE_FP32) {
+            if (g.gn > 0) CK(launch_gridder_fp32(L, b->stream, b->d_gargs.as<GridderArgs>()));
+        } else {
+            TRY(tc_grid_batch(b->d_tg.as<TcArgs>(), L.items, g.gn, b->mode, b->stream, g_last_error));
+        }
     }
-    SubgridOpArgs A{};
-    A.g.S = b->S;
-    A.refs = b->d_refs.as<int2>();
-    A.nsub = b->nrefs;
-    A.wstack = true;
-    CK(launch_subgrid_ifft_add(A, b->stream, b->d_aargs.as<SubgridOpArgs>()));
+    for (const auto &g : b->groups) {
+        SubgridOpArgs A{};
+        A.g.S = g.S;
+        A.refs = b->d_refs.as<int2>() + g.r0;
+        A.nsub = g.rn;
+        A.wstack = true;
+        if (g.rn > 0) CK(launch_subgrid_ifft_add(A, b->stream, b->d_aargs.as<SubgridOpArgs>()));
+    }
     return P9IDG_OK;
 }
 
@@ -993,22 +1002,25 @@ p9idg_status batch_degrid(p9idg_batch *b) {
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(b->d_done.p, b->d_done_init.p, sizeof(int32_t) * n, cudaMemcpyDeviceToDevice, b->stream));
     CK(cudaMemsetAsync(b->d_finish.p, 0, sizeof(unsigned long long) * n, b->stream));
-    SubgridOpArgs A{};
-    A.g.S = b->S;
-    A.refs = b->d_refs.as<int2>();
-    A.nsub = b->nrefs;
-    A.wstack = true;
-    CK(launch_split_subgrid_fft(A, b->stream, b->d_sargs.as<SubgridOpArgs>()));
+    for (const auto &g : b->groups) {
+        SubgridOpArgs A{};
+        A.g.S = g.S;
+        A.refs = b->d_refs.as<int2>() + g.r0;
+        A.nsub = g.rn;
+        A.wstack = true;
+        if (g.rn > 0) CK(launch_split_subgrid_fft(A, b->stream, b->d_sargs.as<SubgridOpArgs>()));
+    }
     for (size_t i = 0; i < n; i++) CK(cudaMemsetAsync(b->vis_out[i], 0, b->vis_bytes[i], b->stream));
-    GridderArgs L{};
-    L.g.S = b->S;
-    L.items = b->d_ditems.as<WorkItem>();
-    L.nitems = b->nditems;
-    if (b->mode == P9IDG_MODE_FP32) {
-        CK(launch_degridder_fp32(L, b->stream, b->d_dargs.as<GridderArgs>()));
-    } else {
-        TRY(tc_degrid_batch(b->d_td.as<TcArgs>(), b->d_ditems.as<WorkItem>(), b->nditems, b->mode, b->stream,
-                            g_last_error));
+    for (const auto &g : b->groups) {
+        GridderArgs L{};
+        L.g.S = g.S;
+        L.items = b->d_ditems.as<WorkItem>() + g.d0;
+        L.nitems = g.dn;
+        if (b->mode == P9IDG_MODE_FP32) {
+            if (g.dn > 0) CK(launch_degridder_fp32(L, b->stream, b->d_dargs.as<GridderArgs>()));
+        } else {
+            TRY(tc_degrid_batch(b->d_td.as<TcArgs>(), L.items, g.dn, b->mode, b->stream, g_last_error));
+        }
     }
     return P9IDG_OK;
 }
@@ -1032,11 +1044,29 @@ p9idg_status batch_order(p9idg_batch *b, int32_t schedule) {
             return pv[x.problem] != pv[y.problem] ? pv[x.problem] < pv[y.problem] : x.problem < y.problem;
         return item_vis(x) > item_vis(y);
     };
+    auto size_of = [&](const WorkItem &w) { return b->plans[w.problem]->c.subgrid_size; };
     for (auto *v : {&b->h_gitems, &b->h_ditems}) {
         if (schedule == P9IDG_SCHEDULE_SMALL_FIRST)
             std::stable_sort(v->begin(), v->end(), small_first);
         else
             std::stable_sort(v->begin(), v->end(), throughput);
+        // one launch per subgrid size: the items of each size contiguous, in size order
+        std::stable_sort(v->begin(), v->end(),
+                         [&](const WorkItem &x, const WorkItem &y) { return size_of(x) < size_of(y); });
+    }
+    for (auto &g : b->groups) {
+        g.g0 = g.gn = g.d0 = g.dn = 0;
+        bool gs = false, ds = false;
+        for (size_t k = 0; k < b->h_gitems.size(); k++)
+            if (size_of(b->h_gitems[k]) == g.S) {
+                if (!gs) g.g0 = static_cast<int32_t>(k), gs = true;
+                g.gn++;
+            }
+        for (size_t k = 0; k < b->h_ditems.size(); k++)
+            if (size_of(b->h_ditems[k]) == g.S) {
+                if (!ds) g.d0 = static_cast<int32_t>(k), ds = true;
+                g.dn++;
+            }
     }
     TRY(upload(b->d_gitems, b->h_gitems));
     TRY(upload(b->d_ditems, b->h_ditems));
@@ -1518,8 +1548,10 @@ p9idg_status p9idg_batch_create(p9idg_plan *const *plans, int32_t nplans, const 
     for (int i = 0; i < nplans; i++) {
         if (!plans[i] || !d_vis[i] || !d_layers[i] || !d_grids[i] || !d_vis_out[i])
             return fail(P9IDG_INVALID_ARGUMENT, "null plan or buffer");
-        if (plans[i]->mode != plans[0]->mode || plans[i]->c.subgrid_size != plans[0]->c.subgrid_size)
-            return fail(P9IDG_UNSUPPORTED, "a batch needs one precision mode and one subgrid size");
+        if (plans[i]->mode != plans[0]->mode)
+            return fail(P9IDG_UNSUPPORTED, "a batch needs one precision mode");
+        if (plans[i]->mode != P9IDG_MODE_FP32 && plans[i]->c.subgrid_size != plans[0]->c.subgrid_size)
+            return fail(P9IDG_UNSUPPORTED, "a tensor-core batch needs one subgrid size");
     }
     auto *b = new (std::nothrow) p9idg_batch();
     if (!b) return fail(P9IDG_OUT_OF_MEMORY, "batch allocation");
@@ -1531,7 +1563,6 @@ p9idg_status p9idg_batch_create(p9idg_plan *const *plans, int32_t nplans, const 
     b->plans.assign(plans, plans + nplans);
     b->mode = plans[0]->mode;
     b->S = plans[0]->c.subgrid_size;
-    const int S = b->S;
     std::vector<GridderArgs> ga(nplans), da(nplans);
     std::vector<SubgridOpArgs> aa(nplans), sa(nplans);
     std::vector<TcArgs> tg(nplans), td(nplans);
@@ -1558,6 +1589,7 @@ p9idg_status p9idg_batch_create(p9idg_plan *const *plans, int32_t nplans, const 
     }
     for (int i = 0; i < nplans; i++) {
         p9idg_plan *p = plans[i];
+        const int S = p->c.subgrid_size;
         cudaError_t e = p->d_partials.ensure(sizeof(float2) * S * S * std::max<size_t>(1, p->nslots));
         if (e == cudaSuccess) e = p->d_subgrids.ensure(sizeof(float2) * S * S * std::max<size_t>(1, p->dsub.size()));
         if (e != cudaSuccess) return bail(cuda_fail(e, "plan buffers"));
@@ -1599,12 +1631,30 @@ p9idg_status p9idg_batch_create(p9idg_plan *const *plans, int32_t nplans, const 
         }
         done[i] = static_cast<int32_t>(dsrc->size());
         for (size_t s = 0; s < p->dsub.size(); s++) refs.push_back(make_int2(i, static_cast<int>(s)));
+        bool known = false;
+        for (const auto &g : b->groups) known |= g.S == S;
+        if (!known) b->groups.push_back({S, 0, 0, 0, 0, 0, 0});
         b->layers.push_back(d_layers[i]);
         b->layer_bytes.push_back(sizeof(float2) * static_cast<size_t>(p->c.wlayer_count) * nn_of(p));
         b->vis_out.push_back(d_vis_out[i]);
         b->vis_bytes.push_back(sizeof(float2) * vis_count_of(p));
         cudaError_t e2 = cudaStreamSynchronize(p->stream);
         if (e2 != cudaSuccess) return bail(cuda_fail(e2, "plan preparation"));
+    }
+    std::sort(b->groups.begin(), b->groups.end(),
+              [](const p9idg_batch::Group &x, const p9idg_batch::Group &y) { return x.S < y.S; });
+    // subgrid references grouped by size (plan order inside a group)
+    std::stable_sort(refs.begin(), refs.end(), [&](const int2 &x, const int2 &y) {
+        return plans[x.x]->c.subgrid_size < plans[y.x]->c.subgrid_size;
+    });
+    for (auto &g : b->groups) {
+        g.r0 = g.rn = 0;
+        bool rs = false;
+        for (size_t k = 0; k < refs.size(); k++)
+            if (plans[refs[k].x]->c.subgrid_size == g.S) {
+                if (!rs) g.r0 = static_cast<int32_t>(k), rs = true;
+                g.rn++;
+            }
     }
     b->prob_vis.assign(nplans, 0);
     for (const WorkItem &w : gitems) b->prob_vis[w.problem] += static_cast<int64_t>(w.nt) * plans[w.problem]->nch;

@@ -45,12 +45,16 @@ __device__ __forceinline__ uint64_t global_ns() {
     return t;
 }
 
-// Bounded wait: gives up after ~limit_ns (or when *abort is set) and returns false.
+// Bounded wait: gives up after ~limit_ns (or when *abort is set) and returns false.  The abort
+// flag and the clock are read once per 16 polls: the flag is a shared-memory load, and the
+// waiting warps' polls compete with the producers' loads and stores for the same pipe.
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int *abort, uint64_t limit_ns) {
     if (mbar_try_wait(bar, parity)) return true;
     const uint64_t t0 = global_ns();
     while (true) {
-        if (mbar_try_wait(bar, parity)) return true;
+#pragma unroll 1
+        for (int k = 0; k < 16; k++)
+            if (mbar_try_wait(bar, parity)) return true;
         if (*abort) return false;
         if (global_ns() - t0 > limit_ns) return false;
     }

@@ -227,17 +227,21 @@ WORKLOADS = {
 }
 
 
-def batched_workloads(n=64, seed=4, subgrid_size=32, w_layers=8):
-    """Independent imaging problems of mixed sizes: images 512^2..2048^2, 200-2000 times,
-    4-32 channels, 16-64 antennas (log-radial within 8 km), 1.5 arcsec cells, the sky of
-    the 3072^2 workload (power-law points + Gaussians)."""
+def batched_workloads(n=64, seed=4, subgrid_size=32, w_layers=8, mix="config"):
+    """Independent imaging problems of mixed sizes, 1.5 arcsec cells, the sky of the 3072^2
+    workload (power-law points + Gaussians), antennas log-radial within 8 km.
+    mix "config": images 512^2..2048^2, 200-2000 times, 4-32 channels, 16-64 antennas.
+    mix "small": images 512^2..1024^2, 200-500 times, 4-16 channels, 16-32 antennas (problems
+    too small to fill the GPU on their own)."""
     rng = np.random.default_rng(seed)
+    lim = dict(config=((256, 1025), (16, 65), (200, 2001), (4, 33)),
+               small=((256, 513), (16, 33), (200, 501), (4, 17)))[mix]
     out = []
     for i in range(n):
-        N = 2 * int(rng.integers(256, 1025))
-        obs = dict(seed=seed * 1000 + i, n_ant=int(rng.integers(16, 65)), array_diameter_m=8000.0,
-                   layout="log_radial", nt=int(rng.integers(200, 2001)), dump_s=10.0, f_lo=1.2e9, f_hi=1.5e9,
-                   nch=int(rng.integers(4, 33)), grid_size=N, cell_arcsec=1.5, n_power_law=2000, n_gauss=20,
+        N = 2 * int(rng.integers(*lim[0]))
+        obs = dict(seed=seed * 1000 + i, n_ant=int(rng.integers(*lim[1])), array_diameter_m=8000.0,
+                   layout="log_radial", nt=int(rng.integers(*lim[2])), dump_s=10.0, f_lo=1.2e9, f_hi=1.5e9,
+                   nch=int(rng.integers(*lim[3])), grid_size=N, cell_arcsec=1.5, n_power_law=2000, n_gauss=20,
                    noise_sigma=1e-3)
         out.append(dict(obs=obs, grid=dict(subgrid_size=subgrid_size, kernel_size=8, max_timesteps=1024,
                                            w_layers=w_layers)))

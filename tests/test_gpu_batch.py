@@ -12,10 +12,12 @@ from conftest import constants, pkg, rel_l2, synth
 pytestmark = pytest.mark.gpu
 
 
-def _problems(torch, mode):
+def _problems(torch, mode, sizes=None):
     specs = [("small_256", dict(n_ant=8, nt=300, nch=8, seed=21), dict(grid_size=256)),
              ("meerkat_3072", dict(n_ant=9, nt=200, nch=12, seed=22), dict(grid_size=1024)),
              ("small_256", dict(n_ant=6, nt=500, nch=4, seed=23), dict(grid_size=384))]
+    if sizes:  # per-problem subgrid size and kernel size
+        specs = [(n, kw, dict(o, subgrid_size=S, kernel_size=k)) for (n, kw, o), (S, k) in zip(specs, sizes)]
     out = []
     for name, kw, over in specs:
         obs, cd = synth.build(synth.scaled_workload(name, **kw))
@@ -28,7 +30,7 @@ def _problems(torch, mode):
                     layers=torch.empty((W, N, N), dtype=torch.complex64, device="cuda"),
                     grid=torch.randn((N, N), dtype=torch.complex64, device="cuda", generator=g),
                     out=torch.empty(obs.vis.shape, dtype=torch.complex64, device="cuda"))
-        out.append((part, cd, bufs))
+        out.append((part, cd, bufs, obs))
     return out
 
 
@@ -38,7 +40,7 @@ def test_batch_matches_single_plans(need_gpu, mode):
     torch = pytest.importorskip("torch")
     probs = _problems(torch, mode)
     refs = []
-    for part, cd, b in probs:
+    for part, cd, b, _ in probs:
         plan = part.plan
         lay = torch.empty_like(b["layers"])
         vo = torch.empty_like(b["out"])
@@ -46,22 +48,22 @@ def test_batch_matches_single_plans(need_gpu, mode):
         plan.degrid_w_device(b["grid"].data_ptr(), vo.data_ptr())
         plan.synchronize()
         refs.append((lay.cpu().numpy(), vo.cpu().numpy()))
-    batch = pkg.Batch([p.plan for p, _, _ in probs], [b["vis"].data_ptr() for _, _, b in probs],
-                      [b["layers"].data_ptr() for _, _, b in probs], [b["grid"].data_ptr() for _, _, b in probs],
-                      [b["out"].data_ptr() for _, _, b in probs])
+    batch = pkg.Batch([p.plan for p, _, _, _ in probs], [b["vis"].data_ptr() for _, _, b, _ in probs],
+                      [b["layers"].data_ptr() for _, _, b, _ in probs], [b["grid"].data_ptr() for _, _, b, _ in probs],
+                      [b["out"].data_ptr() for _, _, b, _ in probs])
     for replay in (False, True):
-        for _, _, b in probs:
+        for _, _, b, _ in probs:
             b["layers"].fill_(7.0)
             b["out"].fill_(7.0)
         if replay:
             batch.capture_graph()
-            for _, _, b in probs:  # the capture ran the batch once: reset outputs before the replay
+            for _, _, b, _ in probs:  # the capture ran the batch once: reset outputs before the replay
                 b["layers"].fill_(7.0)
                 b["out"].fill_(7.0)
         torch.cuda.synchronize()
         batch.run()
         batch.synchronize()
-        for (part, cd, b), (lay, vo) in zip(probs, refs):
+        for (part, cd, b, _), (lay, vo) in zip(probs, refs):
             assert rel_l2(b["layers"].cpu().numpy(), lay) < 1e-6
             assert rel_l2(b["out"].cpu().numpy(), vo) < 1e-6
         lat = batch.latencies_ms()
@@ -73,32 +75,33 @@ def test_small_first_schedule(need_gpu):
     """The SMALL_FIRST order gives the same results and finishes the smallest problem first."""
     torch = pytest.importorskip("torch")
     probs = _problems(torch, pkg.MODE_TC_BF16X3)
-    batch = pkg.Batch([p.plan for p, _, _ in probs], [b["vis"].data_ptr() for _, _, b in probs],
-                      [b["layers"].data_ptr() for _, _, b in probs], [b["grid"].data_ptr() for _, _, b in probs],
-                      [b["out"].data_ptr() for _, _, b in probs])
+    batch = pkg.Batch([p.plan for p, _, _, _ in probs], [b["vis"].data_ptr() for _, _, b, _ in probs],
+                      [b["layers"].data_ptr() for _, _, b, _ in probs], [b["grid"].data_ptr() for _, _, b, _ in probs],
+                      [b["out"].data_ptr() for _, _, b, _ in probs])
     batch.run()
     batch.synchronize()
-    ref = [(b["layers"].cpu().numpy(), b["out"].cpu().numpy()) for _, _, b in probs]
+    ref = [(b["layers"].cpu().numpy(), b["out"].cpu().numpy()) for _, _, b, _ in probs]
     batch.set_schedule(pkg.Batch.SMALL_FIRST)
     batch.capture_graph()
     batch.run()
     batch.synchronize()
-    for (_, _, b), (lay, vo) in zip(probs, ref):
+    for (_, _, b, _), (lay, vo) in zip(probs, ref):
         assert rel_l2(b["layers"].cpu().numpy(), lay) < 1e-6
         assert rel_l2(b["out"].cpu().numpy(), vo) < 1e-6
-    sizes = [p.plan.info()["gridded_visibilities"] for p, _, _ in probs]
+    sizes = [p.plan.info()["gridded_visibilities"] for p, _, _, _ in probs]
     lat = batch.latencies_ms()
     assert lat[int(np.argmin(sizes))] <= lat[int(np.argmax(sizes))]
     batch.destroy()
 
 
-def test_batch_rejects_mixed_subgrid_sizes(need_gpu):
+def test_batch_rejects_mixed_modes(need_gpu):
     torch = pytest.importorskip("torch")
     obs, cd = synth.build(synth.scaled_workload("small_256", n_ant=5, nt=50, nch=4))
     plans = []
-    for S, k in ((32, 8), (16, 4)):
-        c, _ = constants(cd, subgrid_size=S, kernel_size=k)
+    for mode in (pkg.MODE_FP32, pkg.MODE_TC_BF16X3):
+        c, _ = constants(cd)
         plans.append(pkg.Partitioner.CreatePartition(c, obs.uvw, obs.frequencies).plan)
+        plans[-1].set_mode(mode)
     buf = torch.empty(4, dtype=torch.complex64, device="cuda").data_ptr()
     with pytest.raises(pkg.P9IDGError) as e:
         pkg.Batch(plans, [buf] * 2, [buf] * 2, [buf] * 2, [buf] * 2)
@@ -120,3 +123,29 @@ def test_autotune_picks_a_valid_configuration(need_gpu):
     pkg.set_chunking(part.plan, t["gridder_max_vis"], t["degridder_max_vis"])
     after = pkg.IDG.GridW(c, part, obs.vis, obs.uvw, obs.frequencies)
     assert rel_l2(after, before) < 1e-6
+
+
+def test_fp32_batch_mixes_subgrid_sizes_against_the_oracle(need_gpu):
+    """An FP32 batch whose problems use subgrid sizes 16, 24 and 48 (one launch per kernel stage
+    and size) reproduces every problem's GridW and DeGridW of the FP64 oracle."""
+    import oracle
+
+    torch = pytest.importorskip("torch")
+    probs = _problems(torch, pkg.MODE_FP32, sizes=[(16, 4), (48, 8), (24, 8)])
+    batch = pkg.Batch([p.plan for p, _, _, _ in probs], [b["vis"].data_ptr() for _, _, b, _ in probs],
+                      [b["layers"].data_ptr() for _, _, b, _ in probs],
+                      [b["grid"].data_ptr() for _, _, b, _ in probs], [b["out"].data_ptr() for _, _, b, _ in probs])
+    batch.capture_graph()
+    batch.run()
+    batch.synchronize()
+    for part, cd, b, obs in probs:
+        subs = oracle.partition(cd, obs.uvw, obs.frequencies)
+        assert np.array_equal(part.plan.subgrids(), subs)
+        ref = oracle.idg_grid_w(cd, subs, obs.vis.astype(np.complex64).astype(np.complex128), obs.uvw,
+                                obs.frequencies)
+        # the device API leaves the layers shifted (FFT.Shift folded into the adder), as GridW returns them
+        assert rel_l2(b["layers"].cpu().numpy(), ref) < 1e-5
+        grid = b["grid"].cpu().numpy().astype(np.complex128)
+        vref, _ = oracle.idg_degrid(cd, subs, grid, obs.uvw, obs.frequencies, wstack=True)
+        assert rel_l2(b["out"].cpu().numpy(), vref) < 1e-5
+    batch.destroy()
