@@ -18,7 +18,8 @@
 // lo*hi accumulated in FP32 in tensor memory.  The P1 / T1 corrections use hi*hi only.
 //
 // Gridder MMA layout (per stage of 64 visibilities = K64, k = visibility; real and imaginary
-// parts in separate rows, so two visibilities' values pack into one BF16 pair as they are):
+// parts in separate rows; both operands MN-major, so two rows of one visibility pack into one
+// BF16 pair and a lane, owning one visibility, writes 16-byte lines of 8 rows):
 //   A rows (256, y = row % 32):  [Bh_re ; Bh_im ; B1_re ; B1_im ; Bl_re ; Bl_im ; 0 ; 0]
 //       B = B_k(y) = Bh + Bl,  B1 = dw_k B_k(y) (hi only)
 //   B rows (128, x = row % 32):  [Wh_re ; Wh_im ; Wl_re ; Wl_im],  W = vis_k A_k(x) = Wh + Wl
@@ -135,11 +136,6 @@ __device__ __forceinline__ void named_bar(int id, int nthreads) {
     asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
 }
 
-// byte offset of the 16-byte chunk (row, k group) in a K=64 canonical operand tile (8-row
-// groups 1024 bytes apart, k groups of 8 elements 128 bytes apart)
-__device__ __forceinline__ uint32_t chunk_off64(int row, int kg) {
-    return static_cast<uint32_t>((row >> 3) * 1024 + kg * 128 + (row & 7) * 16);
-}
 
 __device__ __forceinline__ void st_shared_v2(uint32_t addr, uint32_t a, uint32_t b) {
     asm volatile("st.shared.v2.b32 [%0], {%1, %2};" ::"r"(addr), "r"(a), "r"(b) : "memory");
@@ -285,7 +281,7 @@ __global__ void __launch_bounds__(kGThreads, 2)
     if (warp == kGMmaWarp) {
         // ---- MMA issuer ----
         if (lane == 0) {
-            constexpr uint32_t id128 = idesc_f16(128, 128, BF16), id64 = idesc_f16(128, 64, BF16);
+            constexpr uint32_t id128 = idesc_f16(128, 128, BF16, true), id64 = idesc_f16(128, 64, BF16, true);
             for (int i = 0; i < nstages; i++) {
                 const int s = i % kGStages;
                 const uint32_t ph = (i / kGStages) & 1;
@@ -391,12 +387,19 @@ __global__ void __launch_bounds__(kGThreads, 2)
         asm volatile("cp.async.wait_all;" ::: "memory");
     } else {
         // ---- producers
-        // Warp w owns k group w (visibilities 8w .. 8w+7 of the stage); lane = row (y, and x).
-        // Each lane stores one 16-byte chunk per operand row: a quarter-warp writes 128
-        // contiguous bytes, and the ring reads are broadcasts.
-        const int yy = lane, kg = warp, kv = kg * 8;
-        const float m_y = a.lmn[yy], g_y = a.tabs[yy];  // y-side tables (l and m coincide, f and g coincide)
-        const float l_x = m_y, f_x = g_y;
+        // Lane = visibility: warp w covers visibilities 32 (w & 1) + lane of each stage and the 8
+        // rows 8 (w >> 1) .. +7 (y on the B side, x on the W side).  A lane loads its own
+        // visibility's coefficients and sample (coalesced: a few shared-memory wavefronts per
+        // warp instead of several per visibility for broadcasts), evaluates the 8 rows, and
+        // stores each operand row group as one 16-byte line of an MN-major core matrix
+        // (8 rows of one k): a warp writes 512 contiguous bytes per row group.
+        const int half = warp & 1, rg = warp >> 1, kl = 32 * half + lane;
+        float mt[8], gt[8];  // m_y and g_y of the 8 rows (l_x and f_x are the same values)
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            mt[j] = a.lmn[8 * rg + j];
+            gt[j] = a.tabs[8 * rg + j];
+        }
         float sv = 1.f;  // FP16: power-of-two scale of this item's visibilities
         if (!BF16) {
             float mx = 0.f;
@@ -417,9 +420,12 @@ __global__ void __launch_bounds__(kGThreads, 2)
                 }
                 break;
             }
-            // the ring slot is released only after the values read from it have been used (below):
-            // an arrive right after the loads could let the next copy into the slot overtake a
-            // shared-memory load still queued, which would then return the next stage's data
+            // the lane's own coefficients and visibility (zeros past the item's end: the loader
+            // writes them so)
+            const float4 c = reinterpret_cast<const float4 *>(ring + slot * kGRingSlot)[kl];
+            const int off = TMA ? static_cast<int>((v0 + i * kGVps) & 1) : 0;
+            const float2 vv = load_vis(reinterpret_cast<const VisT *>(ring + slot * kGRingSlot + kGRingVis) + off, kl);
+            // the ring slot is released only after the values read from it have been used (below)
             if (!warp_wait(&empty[s], ph ^ 1, abort_flag, a.wait_ns)) {
                 if (lane == 0) {
                     *abort_flag = 1;
@@ -427,38 +433,34 @@ __global__ void __launch_bounds__(kGThreads, 2)
                 }
                 break;
             }
-            const float4 *rc = reinterpret_cast<const float4 *>(ring + slot * kGRingSlot) + kv;
-            const int off = TMA ? static_cast<int>((v0 + i * kGVps) & 1) : 0;
-            const VisT *rv = reinterpret_cast<const VisT *>(ring + slot * kGRingSlot + kGRingVis) + off + kv;
-            // words: [pair][row] with row = Bh_re, Bh_im, B1_re, B1_im, Bl_re, Bl_im, Wh_re, Wh_im,
-            // Wl_re, Wl_im; a pair packs visibilities (2p, 2p+1) of this warp's eight
+            const float dws = c.z * sw;
+            const float vre = vv.x * sv, vim = vv.y * sv;
+            // words: [row pair][type] with type = Bh_re, Bh_im, B1_re, B1_im, Bl_re, Bl_im, Wh_re, Wh_im,
+            // Wl_re, Wl_im; a pair packs rows (2p, 2p+1) of the warp's eight
             uint32_t wd[4][10];
 #pragma unroll
             for (int pr = 0; pr < 4; pr++) {
-                float cb[2], sb[2], wre[2], wim[2], dws[2];
+                float cb[2], sb[2], wre[2], wim[2];
 #pragma unroll
                 for (int u = 0; u < 2; u++) {
-                    const int v = 2 * pr + u;
-                    const float4 c = rc[v];
-                    const float2 vv = load_vis(rv, v);
-                    // y side: B_k(y)
-                    __sincosf(fmaf(c.y, m_y, c.z * g_y), &sb[u], &cb[u]);
-                    dws[u] = c.z * sw;
-                    // x side: W = vis * A_k(x)
+                    const int j = 2 * pr + u;
+                    const float zg = c.z * gt[j];
+                    __sincosf(fmaf(c.y, mt[j], zg), &sb[u], &cb[u]);  // B_k(y)
                     float sa, ca;
-                    __sincosf(fmaf(c.x, l_x, c.z * f_x), &sa, &ca);
-                    wre[u] = (vv.x * ca - vv.y * sa) * sv;
-                    wim[u] = (vv.x * sa + vv.y * ca) * sv;
+                    __sincosf(fmaf(c.x, mt[j], zg), &sa, &ca);       // A_k(x)
+                    wre[u] = vre * ca - vim * sa;
+                    wim[u] = vre * sa + vim * ca;
                 }
                 split_pair<BF16>(cb[0], cb[1], wd[pr][0], wd[pr][4]);
                 split_pair<BF16>(sb[0], sb[1], wd[pr][1], wd[pr][5]);
-                wd[pr][2] = Half16<BF16>::pack(dws[0] * cb[0], dws[1] * cb[1]);
-                wd[pr][3] = Half16<BF16>::pack(dws[0] * sb[0], dws[1] * sb[1]);
+                wd[pr][2] = Half16<BF16>::pack(dws * cb[0], dws * cb[1]);
+                wd[pr][3] = Half16<BF16>::pack(dws * sb[0], dws * sb[1]);
                 split_pair<BF16>(wre[0], wre[1], wd[pr][6], wd[pr][8]);
                 split_pair<BF16>(wim[0], wim[1], wd[pr][7], wd[pr][9]);
             }
+            // MN-major: row group G (8 rows) of an operand at G * 1024 bytes, k at 16 k
             const uint32_t A = sbase + s * kGStageBytes, B = A + kGStageA;
-            const uint32_t ko = chunk_off64(yy, kg);
+            const uint32_t ko = static_cast<uint32_t>(rg * kGSbo + kl * 16);
 #define P9_ST(addr, r) st_shared_v4((addr), wd[0][r], wd[1][r], wd[2][r], wd[3][r])
             P9_ST(A + ko, 0);                              // Bh_re: rows 0-31
             P9_ST(A + kGRows32 + ko, 1);                   // Bh_im: rows 32-63
@@ -875,7 +877,7 @@ __global__ void __launch_bounds__(kDThreads, 2)
 
 // ---------------- self-test GEMM: C[128][N] = A[128][64] . B[N][64]^T ----------------
 
-template <bool BF16>
+template <bool BF16, bool MN>
 __global__ void __launch_bounds__(128) tc_selftest_kernel(const float *A, const float *B, int N, float *C,
                                                           int32_t *status) {
     extern __shared__ unsigned char smem_raw[];
@@ -894,10 +896,23 @@ __global__ void __launch_bounds__(128) tc_selftest_kernel(const float *A, const 
         tmem_alloc(tmem_slot, 128);
         tmem_relinquish();
     }
-    // operands: each 16-byte chunk (row, kg) holds 8 consecutive k of one row
+    // operands: K-major, each 16-byte chunk (row, kg) holds 8 consecutive k of one row; MN-major,
+    // each 16-byte chunk (row group g, k) at g * 1024 + 16 k holds 8 consecutive rows of one k
     for (int cc = threadIdx.x; cc < 128 * 8; cc += 128) {
-        const int row = (cc >> 6) * 8 + (cc & 7), kg = (cc >> 3) & 7;
         uint32_t w[4];
+        if (MN) {
+            const int g = cc >> 6, k = cc & 63;
+            for (int u = 0; u < 4; u++)
+                w[u] = Half16<BF16>::pack(A[(8 * g + 2 * u) * 64 + k], A[(8 * g + 2 * u + 1) * 64 + k]);
+            st_shared_v4(smem_u32(sa) + cc * 16, w[0], w[1], w[2], w[3]);
+            if (8 * g < N) {
+                for (int u = 0; u < 4; u++)
+                    w[u] = Half16<BF16>::pack(B[(8 * g + 2 * u) * 64 + k], B[(8 * g + 2 * u + 1) * 64 + k]);
+                st_shared_v4(smem_u32(sb) + cc * 16, w[0], w[1], w[2], w[3]);
+            }
+            continue;
+        }
+        const int row = (cc >> 6) * 8 + (cc & 7), kg = (cc >> 3) & 7;
         for (int u = 0; u < 4; u++)
             w[u] = Half16<BF16>::pack(A[row * 64 + kg * 8 + 2 * u], A[row * 64 + kg * 8 + 2 * u + 1]);
         st_shared_v4(smem_u32(sa) + cc * 16, w[0], w[1], w[2], w[3]);
@@ -913,7 +928,7 @@ __global__ void __launch_bounds__(128) tc_selftest_kernel(const float *A, const 
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
     if (threadIdx.x == 0) {
-        const uint32_t idesc = idesc_f16(128, N, BF16);
+        const uint32_t idesc = idesc_f16(128, N, BF16, MN);
         for (int kc = 0; kc < 4; kc++)
             mma_f16(tmem, smem_desc(smem_u32(sa) + kc * 256, 128, 1024), smem_desc(smem_u32(sb) + kc * 256, 128, 1024),
                     idesc, kc > 0 ? 1u : 0u);
@@ -1354,20 +1369,22 @@ p9idg_status tc_selftest(int mode, int N, double *max_rel_err, std::string &err)
     if (e == cudaSuccess) e = cudaMemcpy(dB, B.data(), B.size() * 4, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemset(dS, 0, 4);
     const uint32_t smem = 2 * 128 * 128 + 64 + 1024;
-    if (e == cudaSuccess) {
-        if (bf16) {
-            e = set_smem(tc_selftest_kernel<true>, smem);
-            if (e == cudaSuccess) tc_selftest_kernel<true><<<1, 128, smem>>>(dA, dB, N, dC, dS);
-        } else {
-            e = set_smem(tc_selftest_kernel<false>, smem);
-            if (e == cudaSuccess) tc_selftest_kernel<false><<<1, 128, smem>>>(dA, dB, N, dC, dS);
-        }
+    std::vector<float> C(128 * N), C2(128 * N);
+    for (int layout = 0; layout < 2 && e == cudaSuccess; layout++) {  // K-major, then MN-major operands
+        auto run = [&](auto kernel) {
+            cudaError_t r = set_smem(kernel, smem);
+            if (r == cudaSuccess) kernel<<<1, 128, smem>>>(dA, dB, N, dC, dS);
+            return r;
+        };
+        if (bf16)
+            e = layout ? run(tc_selftest_kernel<true, true>) : run(tc_selftest_kernel<true, false>);
+        else
+            e = layout ? run(tc_selftest_kernel<false, true>) : run(tc_selftest_kernel<false, false>);
         if (e == cudaSuccess) e = cudaGetLastError();
         if (e == cudaSuccess) e = cudaDeviceSynchronize();
+        if (e == cudaSuccess) e = cudaMemcpy(layout ? C2.data() : C.data(), dC, C.size() * 4, cudaMemcpyDeviceToHost);
     }
-    std::vector<float> C(128 * N);
     int32_t status = 0;
-    if (e == cudaSuccess) e = cudaMemcpy(C.data(), dC, C.size() * 4, cudaMemcpyDeviceToHost);
     if (e == cudaSuccess) e = cudaMemcpy(&status, dS, 4, cudaMemcpyDeviceToHost);
     cudaFree(dA);
     cudaFree(dB);
@@ -1386,7 +1403,7 @@ p9idg_status tc_selftest(int mode, int N, double *max_rel_err, std::string &err)
         for (int j = 0; j < N; j++) {
             double ref = 0;
             for (int k = 0; k < 64; k++) ref += static_cast<double>(A[i * 64 + k]) * B[j * 64 + k];
-            maxerr = std::max(maxerr, std::fabs(ref - C[i * N + j]));
+            maxerr = std::max(maxerr, std::max(std::fabs(ref - C[i * N + j]), std::fabs(ref - C2[i * N + j])));
             maxref = std::max(maxref, std::fabs(ref));
         }
     *max_rel_err = maxerr / std::max(maxref, 1e-30);

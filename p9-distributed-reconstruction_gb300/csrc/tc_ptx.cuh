@@ -1,10 +1,11 @@
 // Inline-PTX wrappers for the sm_100-family tensor-core path: mbarriers, tcgen05 TMEM
 // allocation, MMA issue/commit, TMEM loads, and the shared-memory matrix descriptor.
 //
-// Operand layout used throughout (K-major, no swizzle): an operand tile of R rows and K
-// bf16/fp16 elements is stored as 8-row x 8-element core matrices of 128 contiguous bytes
-// (row r8 at byte 16*r8); core matrix (row group rg, k group kg) sits at
-// rg * SBO + kg * LBO with LBO = 128 and SBO = (K/8) * 128.
+// Operand layouts (no swizzle): an operand tile of R rows (M or N) and K bf16/fp16 elements is
+// stored as 8 x 8-element core matrices of 128 contiguous bytes; core matrix (row group rg,
+// k group kg) sits at rg * SBO + kg * LBO with LBO = 128 and SBO = (K/8) * 128.  K-major: 16-byte
+// lines of 8 consecutive k, one per row (row r8 at byte 16*r8).  MN-major: 16-byte lines of 8
+// consecutive rows, one per k (k8 at byte 16*k8).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -136,9 +137,10 @@ __device__ __forceinline__ void tc_fence_after() {
 
 // ---- tcgen05: MMA ----
 // Instruction descriptor, kind::f16: D = F32, A/B = BF16 (bf16 = true) or F16, both K-major.
-__host__ __device__ constexpr uint32_t idesc_f16(int M, int N, bool bf16) {
-    return (1u << 4) | ((bf16 ? 1u : 0u) << 7) | ((bf16 ? 1u : 0u) << 10) | (static_cast<uint32_t>(N >> 3) << 17) |
-           (static_cast<uint32_t>(M >> 4) << 24);
+// mn_major: both operands MN-major (bits 15 and 16, "transpose A / B").
+__host__ __device__ constexpr uint32_t idesc_f16(int M, int N, bool bf16, bool mn_major = false) {
+    return (1u << 4) | ((bf16 ? 1u : 0u) << 7) | ((bf16 ? 1u : 0u) << 10) | ((mn_major ? 3u : 0u) << 15) |
+           (static_cast<uint32_t>(N >> 3) << 17) | (static_cast<uint32_t>(M >> 4) << 24);
 }
 
 // Shared-memory matrix descriptor (no swizzle).
