@@ -85,6 +85,10 @@ struct Half16<true> {
     }
     static __device__ __forceinline__ float lo_of(uint32_t w) { return __uint_as_float(w << 16); }
     static __device__ __forceinline__ float hi_of(uint32_t w) { return __uint_as_float(w & 0xFFFF0000u); }
+    static __device__ __forceinline__ uint32_t mul2(uint32_t x, uint32_t y) {
+        __nv_bfloat162 r = __hmul2(*reinterpret_cast<__nv_bfloat162 *>(&x), *reinterpret_cast<__nv_bfloat162 *>(&y));
+        return *reinterpret_cast<uint32_t *>(&r);
+    }
 };
 
 template <>
@@ -98,6 +102,10 @@ struct Half16<false> {
     }
     static __device__ __forceinline__ float hi_of(uint32_t w) {
         return __half2float(__ushort_as_half(static_cast<unsigned short>(w >> 16)));
+    }
+    static __device__ __forceinline__ uint32_t mul2(uint32_t x, uint32_t y) {
+        __half2 r = __hmul2(*reinterpret_cast<__half2 *>(&x), *reinterpret_cast<__half2 *>(&y));
+        return *reinterpret_cast<uint32_t *>(&r);
     }
 };
 
@@ -434,6 +442,11 @@ __global__ void __launch_bounds__(kGThreads, 2)
                 break;
             }
             const float dws = c.z * sw;
+            // both halves of a packed pair are rows of this lane's visibility: one dw for the pair,
+            // and the first-order rows dw * Bh are one packed 16-bit multiply of the hi pair (relative
+            // error 2^-8 of a term <= |dw r| <= P9IDG_TC_MAX_W_TERM of the sum: <= 4e-5 at the limit,
+            // 7.8e-6 total error measured there against 7.7e-6 with FP32 products; 2.9 % faster)
+            const uint32_t dw2 = Half16<BF16>::pack(dws, dws);
             const float vre = vv.x * sv, vim = vv.y * sv;
             // words: [row pair][type] with type = Bh_re, Bh_im, B1_re, B1_im, Bl_re, Bl_im, Wh_re, Wh_im,
             // Wl_re, Wl_im; a pair packs rows (2p, 2p+1) of the warp's eight
@@ -453,8 +466,8 @@ __global__ void __launch_bounds__(kGThreads, 2)
                 }
                 split_pair<BF16>(cb[0], cb[1], wd[pr][0], wd[pr][4]);
                 split_pair<BF16>(sb[0], sb[1], wd[pr][1], wd[pr][5]);
-                wd[pr][2] = Half16<BF16>::pack(dws * cb[0], dws * cb[1]);
-                wd[pr][3] = Half16<BF16>::pack(dws * sb[0], dws * sb[1]);
+                wd[pr][2] = Half16<BF16>::mul2(wd[pr][0], dw2);  // dw * Bh (hi only)
+                wd[pr][3] = Half16<BF16>::mul2(wd[pr][1], dw2);
                 split_pair<BF16>(wre[0], wre[1], wd[pr][6], wd[pr][8]);
                 split_pair<BF16>(wim[0], wim[1], wd[pr][7], wd[pr][9]);
             }
