@@ -107,6 +107,60 @@ __global__ void __launch_bounds__(S * S / ppt_for(S))
     }
 }
 
+// One pass of the FP32 degridder over visibility slots k < NK of this thread (b + k * 128 + tid):
+// the phases in FP32 from FP64 coefficients, one sincos per pixel and visibility (Gridder.cs:97-157).
+template <int S, typename OutT, int NK>
+__device__ __forceinline__ void degrid_pass(const GridderArgs &a, const Geometry &g, const DevSubgrid &sg,
+                                            const WorkItem &it, const float4 *s_pix, const float *s_m, double uoff,
+                                            double voff, double woff, int b, int nvis) {
+    const int tid = threadIdx.x;
+    OutT *out = static_cast<OutT *>(a.vis_out);
+    const double *uvw = a.uvw;
+    const double *wn = a.wavenumbers;
+    float du[NK], dv[NK], dw[NK], ar[NK], ai[NK];
+    int64_t idx[NK];
+#pragma unroll
+    for (int k = 0; k < NK; k++) {
+        const int j = b + k * kDegridThreads + tid;
+        ar[k] = ai[k] = 0.f;
+        du[k] = dv[k] = dw[k] = 0.f;
+        idx[k] = -1;
+        if (j < nvis) {
+            const int t = it.t0 + j / g.nch, ch = j - (j / g.nch) * g.nch;
+            const int64_t row = static_cast<int64_t>(sg.bl) * g.nt_all + t;
+            const double *q = uvw + row * 3;
+            const double kw = wn[ch];
+            du[k] = static_cast<float>(uoff - kw * q[0]);
+            dv[k] = static_cast<float>(voff - kw * q[1]);
+            dw[k] = static_cast<float>(woff - kw * q[2]);
+            idx[k] = row * g.nch + ch;
+        }
+    }
+    for (int y = 0; y < S; y++) {
+        const float m = s_m[y];
+        float base[NK];
+#pragma unroll
+        for (int k = 0; k < NK; k++) base[k] = dv[k] * m;
+        const float4 *row = s_pix + y * S;
+#pragma unroll 4
+        for (int x = 0; x < S; x++) {
+            const float4 p = row[x];
+#pragma unroll
+            for (int k = 0; k < NK; k++) {
+                const float ph = fmaf(du[k], p.z, fmaf(dw[k], p.w, base[k]));
+                float sn, cs;
+                __sincosf(ph, &sn, &cs);
+                // pixel * exp(-i ph)   (Gridder.cs:145-147)
+                ar[k] = fmaf(p.x, cs, fmaf(p.y, sn, ar[k]));
+                ai[k] = fmaf(p.y, cs, fmaf(-p.x, sn, ai[k]));
+            }
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < NK; k++)
+        if (idx[k] >= 0) store_vis(out, idx[k], make_float2(ar[k] * g.inv_s2, ai[k] * g.inv_s2));
+}
+
 template <int S, typename OutT, bool BATCH>
 __global__ void __launch_bounds__(kDegridThreads)
     degridder_fp32_kernel(const GridderArgs L, const GridderArgs *__restrict__ probs) {
@@ -132,53 +186,17 @@ __global__ void __launch_bounds__(kDegridThreads)
     const double uoff = static_cast<double>(sg.u + S / 2 - g.N / 2) * g.uv_scale;
     const double voff = static_cast<double>(sg.v + S / 2 - g.N / 2) * g.uv_scale;
     const double woff = 2 * kPi * (static_cast<double>(g.wstep_lambda) * (static_cast<double>(sg.w) + 0.5));
-    OutT *out = static_cast<OutT *>(a.vis_out);
-    const double *uvw = a.uvw;
-    const double *wn = a.wavenumbers;
     const int nvis = it.nt * g.nch;
     for (int b = 0; b < nvis; b += kDegridThreads * kDegridVpt) {
-        float du[kDegridVpt], dv[kDegridVpt], dw[kDegridVpt], ar[kDegridVpt], ai[kDegridVpt];
-        int64_t idx[kDegridVpt];
-#pragma unroll
-        for (int k = 0; k < kDegridVpt; k++) {
-            const int j = b + k * kDegridThreads + tid;
-            ar[k] = ai[k] = 0.f;
-            du[k] = dv[k] = dw[k] = 0.f;
-            idx[k] = -1;
-            if (j < nvis) {
-                const int t = it.t0 + j / g.nch, ch = j - (j / g.nch) * g.nch;
-                const int64_t row = static_cast<int64_t>(sg.bl) * g.nt_all + t;
-                const double *q = uvw + row * 3;
-                const double kw = wn[ch];
-                du[k] = static_cast<float>(uoff - kw * q[0]);
-                dv[k] = static_cast<float>(voff - kw * q[1]);
-                dw[k] = static_cast<float>(woff - kw * q[2]);
-                idx[k] = row * g.nch + ch;
-            }
+        // visibility slots k hold b + k * 128 + tid: only the slots with some visibility left are
+        // evaluated (a block-uniform count; the item's last pass is often short)
+        const int nk = min(kDegridVpt, (nvis - b + kDegridThreads - 1) / kDegridThreads);
+        switch (nk) {
+            case 1: degrid_pass<S, OutT, 1>(a, g, sg, it, s_pix, s_m, uoff, voff, woff, b, nvis); break;
+            case 2: degrid_pass<S, OutT, 2>(a, g, sg, it, s_pix, s_m, uoff, voff, woff, b, nvis); break;
+            case 3: degrid_pass<S, OutT, 3>(a, g, sg, it, s_pix, s_m, uoff, voff, woff, b, nvis); break;
+            default: degrid_pass<S, OutT, kDegridVpt>(a, g, sg, it, s_pix, s_m, uoff, voff, woff, b, nvis); break;
         }
-        for (int y = 0; y < S; y++) {
-            const float m = s_m[y];
-            float base[kDegridVpt];
-#pragma unroll
-            for (int k = 0; k < kDegridVpt; k++) base[k] = dv[k] * m;
-            const float4 *row = s_pix + y * S;
-#pragma unroll 4
-            for (int x = 0; x < S; x++) {
-                const float4 p = row[x];
-#pragma unroll
-                for (int k = 0; k < kDegridVpt; k++) {
-                    const float ph = fmaf(du[k], p.z, fmaf(dw[k], p.w, base[k]));
-                    float sn, cs;
-                    __sincosf(ph, &sn, &cs);
-                    // pixel * exp(-i ph)   (Gridder.cs:145-147)
-                    ar[k] = fmaf(p.x, cs, fmaf(p.y, sn, ar[k]));
-                    ai[k] = fmaf(p.y, cs, fmaf(-p.x, sn, ai[k]));
-                }
-            }
-        }
-#pragma unroll
-        for (int k = 0; k < kDegridVpt; k++)
-            if (idx[k] >= 0) store_vis(out, idx[k], make_float2(ar[k] * g.inv_s2, ai[k] * g.inv_s2));
     }
     if (BATCH) {
         __syncthreads();
