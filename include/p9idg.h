@@ -53,14 +53,18 @@ enum {
 
 /* Largest |dw * r(x, y)| the tensor-core modes accept.  They write the reference's phasor
  * exp(i dw n(x, y)) (Gridder.cs:61-67) as A(x) B(y) exp(i dw r(x, y)), with r the non-separable
- * remainder of the n table (centred on zero), and expand the last factor to first order; the
- * term left out is at most (dw r)^2 / 2 = 5e-5 of each visibility's contribution at this limit,
- * inside the modes' stated 1e-4 relative-L2 bound together with their rounding (~1e-5).  A plan
- * whose gridded samples exceed it keeps the FP32 kernels when a tensor-core mode is selected
- * (p9idg_plan_set_mode returns P9IDG_OK, p9idg_plan_info.mode stays P9IDG_MODE_FP32 and
- * p9idg_last_error() says why); a call whose uvw exceeds it on a tensor-core plan returns
- * P9IDG_UNSUPPORTED. */
+ * remainder of the n table (centred on zero), and expand the last factor in powers of dw r.
+ * First-order form up to P9IDG_TC_MAX_W_TERM: the term left out is at most (dw r)^2 / 2 = 5e-5 of
+ * each visibility's contribution.  Second-order form (two more operand rows per visibility and a third
+ * accumulator block; gridder 8 %, degridder 22 % slower) up to P9IDG_TC_MAX_W_TERM2: the term left out is at most (dw r)^3 / 6 = 4.5e-6.
+ * Both stay inside the modes' stated 1e-4 relative-L2 bound together with their rounding.  A
+ * plan picks the first-order form where it holds, else the second-order one
+ * (p9idg_plan_info.tc_order); a plan beyond P9IDG_TC_MAX_W_TERM2 keeps the FP32 kernels when a
+ * tensor-core mode is selected (p9idg_plan_set_mode returns P9IDG_OK, p9idg_plan_info.mode stays
+ * P9IDG_MODE_FP32 and p9idg_last_error() says why); a call whose uvw exceeds its plan's form
+ * returns P9IDG_UNSUPPORTED. */
 #define P9IDG_TC_MAX_W_TERM 0.01
+#define P9IDG_TC_MAX_W_TERM2 0.03
 
 /* GriddingConstants (Core/ImageDomainGridder/GriddingConstants.cs:33-52).
  * scale_arcsec is the cell size in radians, stored as float like the
@@ -104,6 +108,8 @@ typedef struct p9idg_plan_info {
     int32_t requested_mode;        /* the mode last passed to p9idg_plan_set_mode */
     double tc_w_term;              /* max |dw| * max |r| of the plan's samples (vs P9IDG_TC_MAX_W_TERM);
                                       -1 until a tensor-core mode has been requested */
+    int32_t tc_order;              /* tensor-core form the plan runs: 1 or 2; 0 when it runs FP32 */
+    int32_t reserved;
 } p9idg_plan_info;
 
 /* ---------------- plans: Partitioner ---------------- */
@@ -127,6 +133,10 @@ p9idg_status p9idg_plan_get_info(const p9idg_plan *plan, p9idg_plan_info *out);
 /* Selects the gridder/degridder kernels (P9IDG_MODE_*).  A tensor-core mode on a plan whose
  * w term exceeds P9IDG_TC_MAX_W_TERM keeps the FP32 kernels (see there). */
 p9idg_status p9idg_plan_set_mode(p9idg_plan *plan, int32_t mode);
+/* Tensor-core form: 0 (default) = the first-order form where P9IDG_TC_MAX_W_TERM holds, else the
+ * second-order one; 2 = always the second-order form (smaller error, slower).  No counterpart in
+ * the reference. */
+p9idg_status p9idg_plan_set_tc_order(p9idg_plan *plan, int32_t order);
 /* Subgrid taper float[S][S] applied by gridder and degridder (GriddingConstants.SubgridSpheroidal,
  * Gridder.cs:76,111); NULL restores the identity taper the reference uses. */
 p9idg_status p9idg_plan_set_taper(p9idg_plan *plan, const float *taper);

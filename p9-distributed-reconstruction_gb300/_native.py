@@ -49,11 +49,14 @@ class PlanInfo(ctypes.Structure):
     _fields_ = [("num_subgrids", ctypes.c_int64), ("input_visibilities", ctypes.c_int64),
                 ("gridded_visibilities", ctypes.c_int64), ("work_items", ctypes.c_int64),
                 ("nbl", ctypes.c_int32), ("nt", ctypes.c_int32), ("nch", ctypes.c_int32), ("mode", ctypes.c_int32),
-                ("requested_mode", ctypes.c_int32), ("tc_w_term", ctypes.c_double)]
+                ("requested_mode", ctypes.c_int32), ("tc_w_term", ctypes.c_double), ("tc_order", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
 
 
-# Largest |dw r| the tensor-core modes accept (P9IDG_TC_MAX_W_TERM)
+# Largest |dw r| of the tensor-core forms: first order (P9IDG_TC_MAX_W_TERM) and second order
+# (P9IDG_TC_MAX_W_TERM2)
 TC_MAX_W_TERM = 0.01
+TC_MAX_W_TERM2 = 0.03
 
 
 # name -> (restype, argtypes); every symbol include/p9idg.h declares
@@ -66,6 +69,7 @@ SIGNATURES = {
     "p9idg_plan_get_subgrids": (i32, [P, P, i64]),
     "p9idg_plan_get_info": (i32, [P, ctypes.POINTER(PlanInfo)]),
     "p9idg_plan_set_mode": (i32, [P, i32]),
+    "p9idg_plan_set_tc_order": (i32, [P, i32]),
     "p9idg_plan_set_taper": (i32, [P, P]),
     "p9idg_plan_set_stream": (i32, [P, P]),
     "p9idg_plan_get_stream": (i32, [P, ctypes.POINTER(P)]),

@@ -426,7 +426,7 @@ p9idg_status finish_call(p9idg_plan *p) {
     CK(cudaStreamSynchronize(p->stream));
     if (p->timing) collect_timing(p);
     if (status == kStatusWTerm)
-        return fail(P9IDG_UNSUPPORTED, "this call's uvw puts |dw r| above P9IDG_TC_MAX_W_TERM for the tensor-core "
+        return fail(P9IDG_UNSUPPORTED, "this call's uvw puts |dw r| above the bound of the plan's tensor-core "
                                        "form: use P9IDG_MODE_FP32 or a plan made from this uvw");
     if (status != 0)
         return fail(P9IDG_DEVICE_CHECK_FAILED, "a kernel bounds check tripped (status " + std::to_string(status) + ")");
@@ -959,6 +959,7 @@ struct p9idg_batch {
         int32_t S, g0, gn, d0, dn, r0, rn;
     };
     std::vector<Group> groups;
+    int tc_order = 1;  // tensor-core batches: 2 when any plan needs the second-order form
     std::vector<int64_t> prob_vis;             // visibilities per problem (for the schedules)
     int32_t schedule = P9IDG_SCHEDULE_THROUGHPUT;
     std::vector<void *> layers, vis_out;
@@ -982,7 +983,7 @@ p9idg_status batch_grid(p9idg_batch *b) {
         if (b->mode == P9IDG_MODE_FP32) {
             if (g.gn > 0) CK(launch_gridder_fp32(L, b->stream, b->d_gargs.as<GridderArgs>()));
         } else {
-            TRY(tc_grid_batch(b->d_tg.as<TcArgs>(), L.items, g.gn, b->mode, b->stream, g_last_error));
+            TRY(tc_grid_batch(b->d_tg.as<TcArgs>(), L.items, g.gn, b->mode, b->tc_order, b->stream, g_last_error));
         }
     }
     for (const auto &g : b->groups) {
@@ -1019,7 +1020,8 @@ p9idg_status batch_degrid(p9idg_batch *b) {
         if (b->mode == P9IDG_MODE_FP32) {
             if (g.dn > 0) CK(launch_degridder_fp32(L, b->stream, b->d_dargs.as<GridderArgs>()));
         } else {
-            TRY(tc_degrid_batch(b->d_td.as<TcArgs>(), L.items, g.dn, b->mode, b->stream, g_last_error));
+            TRY(tc_degrid_batch(b->d_td.as<TcArgs>(), L.items, g.dn, b->mode, b->tc_order, b->stream,
+                                g_last_error));
         }
     }
     return P9IDG_OK;
@@ -1166,6 +1168,7 @@ p9idg_status p9idg_plan_get_info(const p9idg_plan *plan, p9idg_plan_info *out) {
     out->mode = plan->mode;
     out->requested_mode = plan->requested_mode;
     out->tc_w_term = plan->tc_w_term;
+    out->tc_order = plan->mode == P9IDG_MODE_FP32 ? 0 : tc_order_for(plan->tc_w_term, plan->tc.want_order);
     return P9IDG_OK;
 }
 
@@ -1182,16 +1185,27 @@ p9idg_status p9idg_plan_set_mode(p9idg_plan *plan, int32_t mode) {
         if (plan->tc_w_term < 0)
             plan->tc_w_term = tc_w_term(plan->subs, plan->lmn, plan->c.subgrid_size, plan->wn, plan->uvw.data(),
                                         plan->nt);
-        if (!(plan->tc_w_term <= P9IDG_TC_MAX_W_TERM)) {
-            // outside the first-order form's error bound: the FP32 kernels grid this plan
+        if (tc_order_for(plan->tc_w_term, plan->tc.want_order) == 0) {
+            // outside both tensor-core forms' error bounds: the FP32 kernels grid this plan
             g_last_error = "tensor-core mode not used: |dw r| = " + std::to_string(plan->tc_w_term) + " > " +
-                           std::to_string(P9IDG_TC_MAX_W_TERM) + " for this plan; it runs the FP32 kernels";
+                           std::to_string(P9IDG_TC_MAX_W_TERM2) + " for this plan; it runs the FP32 kernels";
             mode = P9IDG_MODE_FP32;
         }
     }
     const bool regroup = (plan->mode == P9IDG_MODE_FP32) != (mode == P9IDG_MODE_FP32);
     plan->mode = mode;
     if (regroup) build_gridder_items(plan);
+    return P9IDG_OK;
+}
+
+p9idg_status p9idg_plan_set_tc_order(p9idg_plan *plan, int32_t order) {
+    if (!plan) return fail(P9IDG_INVALID_ARGUMENT, "null plan");
+    if (order != 0 && order != 2) return fail(P9IDG_INVALID_ARGUMENT, "order must be 0 (automatic) or 2");
+    if (plan->tc.ready) {
+        TRY(ensure_device(plan));
+        CK(cudaStreamSynchronize(plan->stream));  // launches in flight use the previous form's limit
+    }
+    tc_set_order(plan->tc, order);
     return P9IDG_OK;
 }
 
@@ -1616,6 +1630,7 @@ p9idg_status p9idg_batch_create(p9idg_plan *const *plans, int32_t nplans, const 
         const std::vector<WorkItem> *dsrc = &p->ditems;
         if (b->mode != P9IDG_MODE_FP32) {
             if ((st = ensure_tc(p)) != P9IDG_OK) return bail(st);
+            b->tc_order = std::max(b->tc_order, p->tc.order);
             if ((st = tc_coefs(p->tc, ga[i], p->stream, g_last_error)) != P9IDG_OK) return bail(st);
             tc_fill_args(p->tc, ga[i], tg[i]);
             tc_fill_args(p->tc, da[i], td[i]);

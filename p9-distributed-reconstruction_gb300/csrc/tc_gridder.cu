@@ -221,12 +221,16 @@ constexpr uint32_t kGStageA = 256 * kGVps * 2;  // MMA1 operand (rows 0-127), th
 constexpr uint32_t kGStageA2 = 128 * kGVps * 2;
 constexpr uint32_t kGStageB = 128 * kGVps * 2;
 constexpr uint32_t kGStageBytes = kGStageA + kGStageB;
-constexpr uint32_t kGEpilogue = 8 * 32 * 33 * 4;  // the epilogue's 8 planes reuse the stages
+constexpr uint32_t kGEpilogue = 12 * 32 * 33 * 4;  // the epilogue's 8 (12) planes reuse the stages
 static_assert(kGEpilogue <= kGStages * kGStageBytes, "epilogue planes must fit in the operand stages");
 constexpr uint32_t kGSmem = kGStages * kGStageBytes + kGRing * kGRingSlot + 512 + 1024;
-constexpr uint32_t kGTmemCols = 128;
+constexpr uint32_t kGTmemCols = 128;   // first order: [Wh | Wl] against the A rows of MMA1 (MMA2 adds in)
+constexpr uint32_t kGTmemCols2 = 256;  // second order: MMA2 (Bl and B2 rows) into its own columns 128-191
 
-template <bool BF16, typename VisT, bool BATCH, bool TMA>
+// O2: the second-order form (|dw r| up to P9IDG_TC_MAX_W_TERM2): rows 192-255 of the A operand,
+// zero in the first-order form, carry B2 = dw^2 Bh, and MMA2 accumulates into its own columns, so
+// P = P0 + i r (.) P1 - (r^2 / 2) (.) P2 with P2 = B diag(vis dw^2) A^T.
+template <bool BF16, typename VisT, bool BATCH, bool TMA, bool O2>
 __global__ void __launch_bounds__(kGThreads, 2)
     tc_gridder_kernel(const TcArgs L, const TcArgs *__restrict__ probs, const __grid_constant__ TmaMaps maps) {
     extern __shared__ unsigned char smem_raw[];
@@ -268,11 +272,11 @@ __global__ void __launch_bounds__(kGThreads, 2)
         mbar_fence_init();
     }
     if (warp == kGMmaWarp) {
-        tmem_alloc(tmem_slot, kGTmemCols);
+        tmem_alloc(tmem_slot, O2 ? kGTmemCols2 : kGTmemCols);
         tmem_relinquish();
     }
     const uint32_t sbase = smem_u32(smem), rbase = smem_u32(ring);
-    if (warp < kGProducerWarps) {
+    if (!O2 && warp < kGProducerWarps) {
         // rows 192-255 of every stage's A operand (MMA2's lower half) stay zero
         constexpr uint32_t kZeroBytes = 64 * kGVps * 2;
         for (uint32_t off = threadIdx.x * 16; off < kGStages * kZeroBytes; off += kGProducerWarps * 32 * 16) {
@@ -304,7 +308,11 @@ __global__ void __launch_bounds__(kGThreads, 2)
                 for (int kc = 0; kc < kGVps / 16; kc++) {
                     const uint64_t db = smem_desc(B + kc * 256, 128, kGSbo);
                     mma_f16(tmem, smem_desc(A + kc * 256, 128, kGSbo), db, id128, (i > 0 || kc > 0) ? 1u : 0u);
-                    mma_f16(tmem, smem_desc(A + kGStageA2 + kc * 256, 128, kGSbo), db, id64, 1u);
+                    if (O2)
+                        mma_f16(tmem + 128, smem_desc(A + kGStageA2 + kc * 256, 128, kGSbo), db, id64,
+                                (i > 0 || kc > 0) ? 1u : 0u);
+                    else
+                        mma_f16(tmem, smem_desc(A + kGStageA2 + kc * 256, 128, kGSbo), db, id64, 1u);
                 }
                 mma_commit(&empty[s]);
             }
@@ -450,7 +458,7 @@ __global__ void __launch_bounds__(kGThreads, 2)
             const float vre = vv.x * sv, vim = vv.y * sv;
             // words: [row pair][type] with type = Bh_re, Bh_im, B1_re, B1_im, Bl_re, Bl_im, Wh_re, Wh_im,
             // Wl_re, Wl_im; a pair packs rows (2p, 2p+1) of the warp's eight
-            uint32_t wd[4][10];
+            uint32_t wd[4][O2 ? 12 : 10];
 #pragma unroll
             for (int pr = 0; pr < 4; pr++) {
                 float cb[2], sb[2], wre[2], wim[2];
@@ -466,8 +474,17 @@ __global__ void __launch_bounds__(kGThreads, 2)
                 }
                 split_pair<BF16>(cb[0], cb[1], wd[pr][0], wd[pr][4]);
                 split_pair<BF16>(sb[0], sb[1], wd[pr][1], wd[pr][5]);
-                wd[pr][2] = Half16<BF16>::mul2(wd[pr][0], dw2);  // dw * Bh (hi only)
-                wd[pr][3] = Half16<BF16>::mul2(wd[pr][1], dw2);
+                if (O2) {  // dw * B rounded once from FP32: the first-order term reaches 0.03 here
+                    wd[pr][2] = Half16<BF16>::pack(dws * cb[0], dws * cb[1]);
+                    wd[pr][3] = Half16<BF16>::pack(dws * sb[0], dws * sb[1]);
+                } else {
+                    wd[pr][2] = Half16<BF16>::mul2(wd[pr][0], dw2);  // dw * Bh (hi only)
+                    wd[pr][3] = Half16<BF16>::mul2(wd[pr][1], dw2);
+                }
+                if (O2) {
+                    wd[pr][O2 ? 10 : 0] = Half16<BF16>::mul2(wd[pr][2], dw2);  // dw^2 * Bh
+                    wd[pr][O2 ? 11 : 1] = Half16<BF16>::mul2(wd[pr][3], dw2);
+                }
                 split_pair<BF16>(wre[0], wre[1], wd[pr][6], wd[pr][8]);
                 split_pair<BF16>(wim[0], wim[1], wd[pr][7], wd[pr][9]);
             }
@@ -481,6 +498,10 @@ __global__ void __launch_bounds__(kGThreads, 2)
             P9_ST(A + 3 * kGRows32 + ko, 3);               // B1_im: rows 96-127
             P9_ST(A + kGStageA2 + ko, 4);                  // Bl_re: rows 128-159
             P9_ST(A + kGStageA2 + kGRows32 + ko, 5);       // Bl_im: rows 160-191
+            if (O2) {
+                P9_ST(A + kGStageA2 + 2 * kGRows32 + ko, O2 ? 10 : 0);  // B2_re: rows 192-223
+                P9_ST(A + kGStageA2 + 3 * kGRows32 + ko, O2 ? 11 : 0);  // B2_im: rows 224-255
+            }
             P9_ST(B + ko, 6);                              // Wh_re: rows 0-31
             P9_ST(B + kGRows32 + ko, 7);                   // Wh_im: rows 32-63
             P9_ST(B + 2 * kGRows32 + ko, 8);               // Wl_re: rows 64-95
@@ -512,6 +533,14 @@ __global__ void __launch_bounds__(kGThreads, 2)
             tmem_ld_wait(r);
 #pragma unroll
             for (int j = 0; j < 32; j++) e[j] += __uint_as_float(r[j]);
+            if (O2) {
+                // MMA2's columns: Bl (quarters 0, 1) adds into P0's plane, B2 (quarters 2, 3) to its own
+                tmem_ld32(t + 128, r);
+                tmem_ld_wait(r);
+                float *e2 = q < 2 ? e : E + (8 + 2 * (q - 2) + h) * 32 * 33 + lane * 33;
+#pragma unroll
+                for (int j = 0; j < 32; j++) e2[j] = (q < 2 ? e2[j] : 0.f) + __uint_as_float(r[j]);
+            }
         }
         tc_fence_before();
         named_bar(1, kGProducerWarps * 32);
@@ -524,7 +553,7 @@ __global__ void __launch_bounds__(kGThreads, 2)
                 ep_t[k] = a.taper[p];
             }
             float2 *out = a.partials + static_cast<int64_t>(it.slot) * kS * kS;
-            const float i0 = 1.f / sv, i1 = 1.f / (sv * sw);  // exact: powers of two
+            const float i0 = 1.f / sv, i1 = 1.f / (sv * sw), i2 = 0.5f / (sv * sw * sw);  // exact: powers of two
 #pragma unroll
             for (int k = 0; k < 4; k++) {
                 const int p = threadIdx.x + k * kGProducerWarps * 32;
@@ -535,7 +564,12 @@ __global__ void __launch_bounds__(kGThreads, 2)
                 const float p1re = (E[4 * 1056 + e] - E[7 * 1056 + e]) * i1;
                 const float p1im = (E[5 * 1056 + e] + E[6 * 1056 + e]) * i1;
                 const float rr = ep_r[k], tap = ep_t[k];
-                const float re = fmaf(-rr, p1im, p0re), im = fmaf(rr, p1re, p0im);
+                float re = fmaf(-rr, p1im, p0re), im = fmaf(rr, p1re, p0im);
+                if (O2) {  // - (r^2 / 2) P2
+                    const float h2 = rr * rr * i2;
+                    re = fmaf(-h2, E[8 * 1056 + e] - E[11 * 1056 + e], re);
+                    im = fmaf(-h2, E[9 * 1056 + e] + E[10 * 1056 + e], im);
+                }
                 out[((y + kS / 2) % kS) * kS + (x + kS / 2) % kS] = make_float2(re * tap, im * tap);
             }
         }
@@ -544,7 +578,7 @@ __global__ void __launch_bounds__(kGThreads, 2)
     __syncthreads();
     if (warp == kGMmaWarp) {
         tc_fence_after();
-        tmem_dealloc(tmem, kGTmemCols);
+        tmem_dealloc(tmem, O2 ? kGTmemCols2 : kGTmemCols);
     }
 }
 
@@ -560,19 +594,26 @@ constexpr int kDLoaderWarp = 9;
 constexpr int kDThreads = 10 * 32;
 constexpr int kDRing = 4;
 constexpr uint32_t kDRingSlot = kDTile * 16;
-constexpr uint32_t kDStatic = 192 * 64 * 2;
+constexpr uint32_t kDStatic = 192 * 64 * 2;   // static B operand: [B0_lo; B0_hi; B1_hi]
+constexpr uint32_t kDStatic2 = 256 * 64 * 2;  // second order: [B0_lo; B0_hi; B1_hi; B2_hi]
 constexpr uint32_t kDTileHalf = 128 * 64 * 2;  // hi (or lo) operand of one tile
 constexpr uint32_t kDTileBytes = 2 * kDTileHalf;
 constexpr uint32_t kDSmem = kDStatic + 2 * kDTileBytes + kDRing * kDRingSlot + 256 + 512 + 1024;
+constexpr uint32_t kDSmem2 = kDStatic2 + 2 * kDTileBytes + kDRing * kDRingSlot + 256 + 512 + 1024;
 constexpr uint32_t kDTmemCols = 256;
 
-template <bool BF16, typename OutT, bool BATCH, bool TMA>
+// O2: the second-order form: vis = S^-2 sum_y conj(B(y)) [T0 - i dw T1 - (dw^2 / 2) T2] with
+// T2 = (r^2 (.) pix) conj(A); MMA1 covers [T0 | T1 | T2] (N = 192) in one accumulator of 192
+// columns (the two accumulators of the first-order form would need 384), so the MMA of tile i + 1
+// waits for the epilogue of tile i.
+template <bool BF16, typename OutT, bool BATCH, bool TMA, bool O2>
 __global__ void __launch_bounds__(kDThreads, 2)
     tc_degridder_kernel(const TcArgs L, const TcArgs *__restrict__ probs, const __grid_constant__ TmaMaps maps) {
+    constexpr int NB = O2 ? 1 : 2;  // accumulator buffers
     extern __shared__ unsigned char smem_raw[];
     unsigned char *smem = smem_1k(smem_raw);
     unsigned char *bstat = smem;
-    unsigned char *tiles = smem + kDStatic;
+    unsigned char *tiles = smem + (O2 ? kDStatic2 : kDStatic);
     unsigned char *ring = tiles + 2 * kDTileBytes;
     float *tab_m = reinterpret_cast<float *>(ring + kDRing * kDRingSlot);  // m[32], g[32]
     float *tab_g = tab_m + kS;
@@ -634,7 +675,7 @@ __global__ void __launch_bounds__(kDThreads, 2)
         }
         const float sr = BF16 ? 1.f : a.r_scale;
         const uint32_t bs = smem_u32(bstat);
-        for (int cc = threadIdx.x; cc < 192 * 8; cc += 256) {
+        for (int cc = threadIdx.x; cc < (O2 ? 256 : 192) * 8; cc += 256) {
             const int cm = cc >> 3, r8 = cc & 7;
             const int row = (cm >> 3) * 8 + r8, kg = cm & 7;
             const int blk = row >> 6, rr = row & 63, y = rr >> 1, p = rr & 1;
@@ -646,10 +687,14 @@ __global__ void __launch_bounds__(kDThreads, 2)
                 const float2 d = data[((y + kS / 2) % kS) * kS + (x + kS / 2) % kS];
                 const float tap = a.taper[pi] * sq;
                 float qre = tap * d.x, qim = tap * d.y;
-                if (blk == 2) {
+                if (blk >= 2) {  // r (.) pix, and r^2 (.) pix for block 3
                     const float rr2 = a.tabs[kS + pi] * sr;
                     qre *= rr2;
                     qim *= rr2;
+                    if (blk == 3) {
+                        qre *= rr2;
+                        qim *= rr2;
+                    }
                 }
                 // p = re: (Q_re, Q_im);  p = im: (Q_im, -Q_re)
                 const float e0 = p == 0 ? qre : qim, e1 = p == 0 ? qim : -qre;
@@ -671,29 +716,29 @@ __global__ void __launch_bounds__(kDThreads, 2)
     if (warp == kDMmaWarp) {
         // ---- MMA issuer
         if (lane == 0) {
-            constexpr uint32_t id128 = idesc_f16(128, 128, BF16), id64 = idesc_f16(128, 64, BF16);
+            constexpr uint32_t id1 = idesc_f16(128, O2 ? 192 : 128, BF16), id64 = idesc_f16(128, 64, BF16);
             for (int i = 0; i < ntiles; i++) {
-                const int b = i & 1;
-                const uint32_t ph = (i >> 1) & 1;
+                const int b = i & 1, cb = i % NB;
+                const uint32_t ph = (i >> 1) & 1, cph = (i / NB) & 1;
                 if (!mbar_wait(&a_full[b], ph, abort_flag, a.wait_ns) ||
-                    !mbar_wait(&acc_empty[b], ph ^ 1, abort_flag, a.wait_ns)) {
+                    !mbar_wait(&acc_empty[cb], cph ^ 1, abort_flag, a.wait_ns)) {
                     *abort_flag = 1;
                     atomicOr(a.status, kStatusWait);
                     break;
                 }
                 tc_fence_after();
                 const uint32_t ahi = ts + b * kDTileBytes, alo = ahi + kDTileHalf;
-                const uint32_t acc = tmem + static_cast<uint32_t>(b * 128);
+                const uint32_t acc = tmem + static_cast<uint32_t>(cb * 128);
 #pragma unroll
                 for (int kc = 0; kc < 4; kc++) {
                     const uint64_t dahi = smem_desc(ahi + kc * 256, 128, 1024);
-                    mma_f16(acc, dahi, smem_desc(bs + 8 * 1024 + kc * 256, 128, 1024), id128, kc > 0 ? 1u : 0u);
+                    mma_f16(acc, dahi, smem_desc(bs + 8 * 1024 + kc * 256, 128, 1024), id1, kc > 0 ? 1u : 0u);
                     mma_f16(acc, dahi, smem_desc(bs + kc * 256, 128, 1024), id64, 1u);
                     mma_f16(acc, smem_desc(alo + kc * 256, 128, 1024), smem_desc(bs + 8 * 1024 + kc * 256, 128, 1024),
                             id64, 1u);
                 }
                 mma_commit(&a_empty[b]);
-                mma_commit(&acc_full[b]);
+                mma_commit(&acc_full[cb]);
                 if (b == 0) drain_phase++;
             }
             // drain: every issued MMA finished before the TMEM is released
@@ -814,8 +859,8 @@ __global__ void __launch_bounds__(kDThreads, 2)
         const int q = warp & 3;
         OutT *out = static_cast<OutT *>(a.vis_out) + (static_cast<int64_t>(sg.bl) * g.nt_all + it.t0) * g.nch;
         for (int i = 0; i < ntiles; i++) {
-            const int b = i & 1, slot = i % kDRing;
-            const uint32_t ph = (i >> 1) & 1, iph = (i / kDRing) & 1;
+            const int b = i % NB, slot = i % kDRing;
+            const uint32_t ph = (i / NB) & 1, iph = (i / kDRing) & 1;
             const int row = q * 32 + lane, j = i * kDTile + row;
             if (!warp_wait(&in_full[slot], iph, abort_flag, a.wait_ns)) {
                 if (lane == 0) {
@@ -837,8 +882,36 @@ __global__ void __launch_bounds__(kDThreads, 2)
             const float dwe = BF16 ? c.z : c.z / a.r_scale;  // T1 was formed from r * r_scale
             const uint32_t acc = tmem + (static_cast<uint32_t>(32 * q) << 16) + static_cast<uint32_t>(b * 128);
             float vre[2] = {0.f, 0.f}, vim[2] = {0.f, 0.f};  // even and odd rows: two independent chains
+            if (O2) {
+                // z = T0 - i dw T1 - (dw^2 / 2) T2, 8 rows (16 columns) of each block at a time
+                const float hd2 = 0.5f * dwe * dwe;  // T2 was formed from r^2 * r_scale^2
 #pragma unroll
-            for (int h = 0; h < 2; h++) {
+                for (int h = 0; h < 4; h++) {
+                    uint32_t t0[16], t1[16], t2[16];
+                    tmem_ld16(acc + h * 16, t0);
+                    tmem_ld16(acc + 64 + h * 16, t1);
+                    tmem_ld16(acc + 128 + h * 16, t2);
+                    tmem_ld_wait(t0);
+                    tmem_ld_wait(t1);
+                    tmem_ld_wait(t2);
+#pragma unroll
+                    for (int yy = 0; yy < 8; yy++) {
+                        const int y = h * 8 + yy;
+                        const float t0re = __uint_as_float(t0[2 * yy]), t0im = __uint_as_float(t0[2 * yy + 1]);
+                        const float t1re = __uint_as_float(t1[2 * yy]), t1im = __uint_as_float(t1[2 * yy + 1]);
+                        const float t2re = __uint_as_float(t2[2 * yy]), t2im = __uint_as_float(t2[2 * yy + 1]);
+                        const float zre = fmaf(-hd2, t2re, fmaf(dwe, t1im, t0re));
+                        const float zim = fmaf(-hd2, t2im, fmaf(-dwe, t1re, t0im));
+                        float sb, cb;
+                        const float my = BATCH ? tab_m[y] : L.m_tab[y], gy = BATCH ? tab_g[y] : L.g_tab[y];
+                        __sincosf(fmaf(c.y, my, c.z * gy), &sb, &cb);
+                        vre[yy & 1] = fmaf(cb, zre, fmaf(sb, zim, vre[yy & 1]));
+                        vim[yy & 1] = fmaf(cb, zim, fmaf(-sb, zre, vim[yy & 1]));
+                    }
+                }
+            }
+#pragma unroll
+            for (int h = 0; h < (O2 ? 0 : 2); h++) {
                 uint32_t t0[32], t1[32];
                 tmem_ld32(acc + h * 32, t0);
                 tmem_ld32(acc + 64 + h * 32, t1);
@@ -997,6 +1070,19 @@ void fill_args(TcArgs &t, const GridderArgs &a, const TcPlanState &st) {
 
 bool tc_subgrid_size_supported(int S) { return S == kS; }
 
+int tc_order_for(double w_term, int want_order) {
+    if (want_order != 2 && w_term <= P9IDG_TC_MAX_W_TERM) return 1;
+    if (w_term <= P9IDG_TC_MAX_W_TERM2) return 2;
+    return 0;
+}
+
+void tc_set_order(TcPlanState &st, int want_order) {
+    st.want_order = want_order;
+    st.order = tc_order_for(st.max_w_r, want_order);
+    const double limit = st.order == 1 ? P9IDG_TC_MAX_W_TERM : P9IDG_TC_MAX_W_TERM2;
+    st.dw_limit = st.r_max > 0 ? limit / st.r_max : INFINITY;
+}
+
 void tc_debug_set(uint64_t wait_ns, int32_t skip_stage) {
     g_wait_ns.store(wait_ns > 0 ? wait_ns : kWaitNs);
     g_skip_stage.store(skip_stage);
@@ -1076,7 +1162,8 @@ p9idg_status tc_prepare(TcPlanState &st, const std::vector<p9idg_subgrid> &subs,
     double wmax, kmax;
     w_k_max(subs, wn, uvw_host, nt_all, wmax, kmax);
     st.max_w_r = wmax * kmax * rmax;
-    st.dw_limit = rmax > 0 ? P9IDG_TC_MAX_W_TERM / rmax : INFINITY;
+    st.r_max = rmax;
+    tc_set_order(st, st.want_order);
     for (int i = 0; i < S; i++) {
         st.m_tab[i] = lmn[i];
         st.g_tab[i] = tabs[i];
@@ -1090,9 +1177,9 @@ p9idg_status tc_prepare(TcPlanState &st, const std::vector<p9idg_subgrid> &subs,
     };
     st.dw_scale = pow2_below(wmax * kmax * 1.0001);
     st.r_scale = pow2_below(rmax);
-    if (!(st.max_w_r <= P9IDG_TC_MAX_W_TERM)) {
-        err = "w term too large for the first-order separable tensor-core form (|dw r| = " +
-              std::to_string(st.max_w_r) + " > " + std::to_string(P9IDG_TC_MAX_W_TERM) + ")";
+    if (st.order == 0) {
+        err = "w term too large for the separable tensor-core forms (|dw r| = " + std::to_string(st.max_w_r) +
+              " > " + std::to_string(P9IDG_TC_MAX_W_TERM2) + ")";
         return P9IDG_UNSUPPORTED;
     }
     // degridder work items: whole time samples, up to degrid_chunk visibilities each
@@ -1145,26 +1232,28 @@ static p9idg_status launch_coef(TcPlanState &st, const GridderArgs &a, int32_t n
 
 namespace {
 
-template <bool BF16, typename VisT, bool BATCH, bool TMA>
+template <bool BF16, typename VisT, bool BATCH, bool TMA, bool O2>
 cudaError_t run_gridder(const TcArgs &t, const TcArgs *probs, int32_t nitems, const TmaMaps &maps,
                         cudaStream_t stream) {
-    cudaError_t e = set_smem(tc_gridder_kernel<BF16, VisT, BATCH, TMA>, kGSmem);
-    if (e == cudaSuccess) tc_gridder_kernel<BF16, VisT, BATCH, TMA><<<nitems, kGThreads, kGSmem, stream>>>(t, probs, maps);
+    cudaError_t e = set_smem(tc_gridder_kernel<BF16, VisT, BATCH, TMA, O2>, kGSmem);
+    if (e == cudaSuccess)
+        tc_gridder_kernel<BF16, VisT, BATCH, TMA, O2><<<nitems, kGThreads, kGSmem, stream>>>(t, probs, maps);
     return e;
 }
 
-template <bool BF16, typename OutT, bool BATCH, bool TMA>
+template <bool BF16, typename OutT, bool BATCH, bool TMA, bool O2>
 cudaError_t run_degridder(const TcArgs &t, const TcArgs *probs, int32_t nitems, const TmaMaps &maps,
                           cudaStream_t stream) {
-    cudaError_t e = set_smem(tc_degridder_kernel<BF16, OutT, BATCH, TMA>, kDSmem);
+    constexpr uint32_t smem = O2 ? kDSmem2 : kDSmem;
+    cudaError_t e = set_smem(tc_degridder_kernel<BF16, OutT, BATCH, TMA, O2>, smem);
     if (e == cudaSuccess)
-        tc_degridder_kernel<BF16, OutT, BATCH, TMA><<<nitems, kDThreads, kDSmem, stream>>>(t, probs, maps);
+        tc_degridder_kernel<BF16, OutT, BATCH, TMA, O2><<<nitems, kDThreads, smem, stream>>>(t, probs, maps);
     return e;
 }
 
 // maps: TMA staging for a single-plan launch (nullptr: cp.async staging).  Batched launches read
 // per-problem buffers and always use cp.async.
-template <bool BATCH>
+template <bool BATCH, bool O2>
 p9idg_status launch_tc_gridder(const TcArgs &t, const TcArgs *probs, int32_t nitems, bool c128, int mode,
                                const TmaMaps *maps, cudaStream_t stream, std::string &err) {
     if (nitems == 0) return P9IDG_OK;
@@ -1175,20 +1264,20 @@ p9idg_status launch_tc_gridder(const TcArgs &t, const TcArgs *probs, int32_t nit
     bool done = false;
     if constexpr (!BATCH) {
         if (maps && !c128) {
-            e = bf16 ? run_gridder<true, float2, false, true>(t, probs, nitems, m, stream)
-                     : run_gridder<false, float2, false, true>(t, probs, nitems, m, stream);
+            e = bf16 ? run_gridder<true, float2, false, true, O2>(t, probs, nitems, m, stream)
+                     : run_gridder<false, float2, false, true, O2>(t, probs, nitems, m, stream);
             done = true;
         }
     }
     if (!done) {
         if (bf16 && c128)
-            e = run_gridder<true, double2, BATCH, false>(t, probs, nitems, m, stream);
+            e = run_gridder<true, double2, BATCH, false, O2>(t, probs, nitems, m, stream);
         else if (bf16)
-            e = run_gridder<true, float2, BATCH, false>(t, probs, nitems, m, stream);
+            e = run_gridder<true, float2, BATCH, false, O2>(t, probs, nitems, m, stream);
         else if (c128)
-            e = run_gridder<false, double2, BATCH, false>(t, probs, nitems, m, stream);
+            e = run_gridder<false, double2, BATCH, false, O2>(t, probs, nitems, m, stream);
         else
-            e = run_gridder<false, float2, BATCH, false>(t, probs, nitems, m, stream);
+            e = run_gridder<false, float2, BATCH, false, O2>(t, probs, nitems, m, stream);
     }
     if (e == cudaSuccess) e = cudaGetLastError();
     if (e != cudaSuccess) {
@@ -1198,7 +1287,7 @@ p9idg_status launch_tc_gridder(const TcArgs &t, const TcArgs *probs, int32_t nit
     return P9IDG_OK;
 }
 
-template <bool BATCH>
+template <bool BATCH, bool O2>
 p9idg_status launch_tc_degridder(const TcArgs &t, const TcArgs *probs, int32_t nitems, bool c128, int mode,
                                  const TmaMaps *maps, cudaStream_t stream, std::string &err) {
     if (nitems == 0) return P9IDG_OK;
@@ -1210,25 +1299,25 @@ p9idg_status launch_tc_degridder(const TcArgs &t, const TcArgs *probs, int32_t n
     if constexpr (!BATCH) {
         if (maps) {
             if (bf16 && c128)
-                e = run_degridder<true, double2, false, true>(t, probs, nitems, m, stream);
+                e = run_degridder<true, double2, false, true, O2>(t, probs, nitems, m, stream);
             else if (bf16)
-                e = run_degridder<true, float2, false, true>(t, probs, nitems, m, stream);
+                e = run_degridder<true, float2, false, true, O2>(t, probs, nitems, m, stream);
             else if (c128)
-                e = run_degridder<false, double2, false, true>(t, probs, nitems, m, stream);
+                e = run_degridder<false, double2, false, true, O2>(t, probs, nitems, m, stream);
             else
-                e = run_degridder<false, float2, false, true>(t, probs, nitems, m, stream);
+                e = run_degridder<false, float2, false, true, O2>(t, probs, nitems, m, stream);
             done = true;
         }
     }
     if (!done) {
         if (bf16 && c128)
-            e = run_degridder<true, double2, BATCH, false>(t, probs, nitems, m, stream);
+            e = run_degridder<true, double2, BATCH, false, O2>(t, probs, nitems, m, stream);
         else if (bf16)
-            e = run_degridder<true, float2, BATCH, false>(t, probs, nitems, m, stream);
+            e = run_degridder<true, float2, BATCH, false, O2>(t, probs, nitems, m, stream);
         else if (c128)
-            e = run_degridder<false, double2, BATCH, false>(t, probs, nitems, m, stream);
+            e = run_degridder<false, double2, BATCH, false, O2>(t, probs, nitems, m, stream);
         else
-            e = run_degridder<false, float2, BATCH, false>(t, probs, nitems, m, stream);
+            e = run_degridder<false, float2, BATCH, false, O2>(t, probs, nitems, m, stream);
     }
     if (e == cudaSuccess) e = cudaGetLastError();
     if (e != cudaSuccess) {
@@ -1314,7 +1403,10 @@ p9idg_status tc_grid(TcPlanState &st, const GridderArgs &a, int mode, cudaStream
     const int64_t nvis = static_cast<int64_t>(a.g.nbl) * a.g.nt_all * a.g.nch;
     const bool tma =
         !a.vis_c128 && make_maps(maps, static_cast<const float4 *>(st.coef), st.ncoef, kGVps, a.vis, nvis);
-    return launch_tc_gridder<false>(t, nullptr, a.nitems, a.vis_c128, mode, tma ? &maps : nullptr, stream, err);
+    return st.order == 2 ? launch_tc_gridder<false, true>(t, nullptr, a.nitems, a.vis_c128, mode, tma ? &maps : nullptr,
+                                                          stream, err)
+                         : launch_tc_gridder<false, false>(t, nullptr, a.nitems, a.vis_c128, mode,
+                                                           tma ? &maps : nullptr, stream, err);
 }
 
 p9idg_status tc_degrid(TcPlanState &st, const GridderArgs &a, int mode, cudaStream_t stream, std::string &err) {
@@ -1325,21 +1417,26 @@ p9idg_status tc_degrid(TcPlanState &st, const GridderArgs &a, int mode, cudaStre
     t.items = static_cast<const WorkItem *>(st.ditems);
     TmaMaps maps;
     const bool tma = make_maps(maps, static_cast<const float4 *>(st.coef), st.ncoef, kDTile, nullptr, 0);
-    return launch_tc_degridder<false>(t, nullptr, st.nditems, a.out_c128, mode, tma ? &maps : nullptr, stream, err);
+    return st.order == 2 ? launch_tc_degridder<false, true>(t, nullptr, st.nditems, a.out_c128, mode,
+                                                            tma ? &maps : nullptr, stream, err)
+                         : launch_tc_degridder<false, false>(t, nullptr, st.nditems, a.out_c128, mode,
+                                                             tma ? &maps : nullptr, stream, err);
 }
 
-p9idg_status tc_grid_batch(const TcArgs *probs, const WorkItem *items, int32_t nitems, int mode,
+p9idg_status tc_grid_batch(const TcArgs *probs, const WorkItem *items, int32_t nitems, int mode, int order,
                            cudaStream_t stream, std::string &err) {
     TcArgs t{};
     t.items = items;
-    return launch_tc_gridder<true>(t, probs, nitems, false, mode, nullptr, stream, err);
+    return order == 2 ? launch_tc_gridder<true, true>(t, probs, nitems, false, mode, nullptr, stream, err)
+                      : launch_tc_gridder<true, false>(t, probs, nitems, false, mode, nullptr, stream, err);
 }
 
-p9idg_status tc_degrid_batch(const TcArgs *probs, const WorkItem *items, int32_t nitems, int mode,
+p9idg_status tc_degrid_batch(const TcArgs *probs, const WorkItem *items, int32_t nitems, int mode, int order,
                              cudaStream_t stream, std::string &err) {
     TcArgs t{};
     t.items = items;
-    return launch_tc_degridder<true>(t, probs, nitems, false, mode, nullptr, stream, err);
+    return order == 2 ? launch_tc_degridder<true, true>(t, probs, nitems, false, mode, nullptr, stream, err)
+                      : launch_tc_degridder<true, false>(t, probs, nitems, false, mode, nullptr, stream, err);
 }
 
 void tc_release(TcPlanState &st) {

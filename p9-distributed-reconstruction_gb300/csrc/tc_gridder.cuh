@@ -24,8 +24,11 @@ struct TcPlanState {
     int32_t nditems = 0;
     std::vector<WorkItem> ditems_host;  // the same list on the host (batches merge them)
     int64_t degrid_chunk = 8192;        // visibilities per degridder work item (set before tc_prepare)
-    double max_w_r = 0;           // max |dw| * max |r|: bound on the phase the first-order form expands
-    double dw_limit = 0;          // P9IDG_TC_MAX_W_TERM / max |r|: the largest |dw| a visibility may have
+    double max_w_r = 0;           // max |dw| * max |r|: bound on the phase the form expands
+    double r_max = 0;             // max |r| of the centred remainder table
+    int want_order = 0;           // 0: the lowest order whose bound holds; 2: always the second-order form
+    int order = 1;                // the form the kernels run: 1 (first order) or 2 (second order)
+    double dw_limit = 0;          // limit of the form / max |r|: the largest |dw| a visibility may have
     float dw_scale = 1.f;         // FP16 mode: power of two with max |dw| * dw_scale < 1
     float r_scale = 1.f;          // FP16 mode: power of two with max |r| * r_scale < 1
     float m_tab[32] = {}, g_tab[32] = {};  // m_y and g_y (the same values serve l_x and f_x)
@@ -72,10 +75,17 @@ void tc_fill_args(const TcPlanState &st, const GridderArgs &a, TcArgs &t);
 p9idg_status tc_coefs(TcPlanState &st, const GridderArgs &a, cudaStream_t stream, std::string &err);
 // One launch over the work items of many problems; `probs` is a device array of TcArgs
 // indexed by WorkItem::problem.
-p9idg_status tc_grid_batch(const TcArgs *probs, const WorkItem *items, int32_t nitems, int mode,
+// order: 2 when any problem of the batch needs the second-order form (it serves first-order
+// problems as well, a little more accurately).
+p9idg_status tc_grid_batch(const TcArgs *probs, const WorkItem *items, int32_t nitems, int mode, int order,
                            cudaStream_t stream, std::string &err);
-p9idg_status tc_degrid_batch(const TcArgs *probs, const WorkItem *items, int32_t nitems, int mode,
+p9idg_status tc_degrid_batch(const TcArgs *probs, const WorkItem *items, int32_t nitems, int mode, int order,
                              cudaStream_t stream, std::string &err);
+// The form (1 or 2) a plan with this w term runs for a requested order (0 = automatic), or 0 when
+// neither bound holds (the plan then keeps the FP32 kernels).
+int tc_order_for(double w_term, int want_order);
+// Re-selects the form of a prepared state after p9idg_plan_set_tc_order (no device work).
+void tc_set_order(TcPlanState &st, int want_order);
 // Builds the tables and uploads them (once per plan).
 p9idg_status tc_prepare(TcPlanState &st, const std::vector<p9idg_subgrid> &subs, const std::vector<float> &lmn,
                         int S, int nch, const std::vector<double> &wn, const double *uvw_host, int nt_all,

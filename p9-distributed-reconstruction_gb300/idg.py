@@ -178,6 +178,10 @@ class Plan:
         _check(nat.lib().p9idg_plan_set_mode(self.handle, int(mode)))
         return self.info()["mode"]
 
+    def set_tc_order(self, order: int):
+        """Tensor-core form: 0 = automatic (first order where its bound holds), 2 = second order."""
+        _check(nat.lib().p9idg_plan_set_tc_order(self.handle, int(order)))
+
     def set_taper(self, taper):
         t = None if taper is None else np.ascontiguousarray(taper, np.float32)
         _check(nat.lib().p9idg_plan_set_taper(self.handle, _ptr(t)))
