@@ -30,7 +30,9 @@
 //   P0 = sum over the W column blocks of (re.re - im.im, re.im + im.re) of lanes 0-63,
 //   P1 the same of lanes 64-127.
 // Degridder (per tile of 128 visibilities = rows; k = 2x + re/im):
-//   A rows: [cos, sin](phase_A);  static B rows (192, row 2y+p):  [B0_lo ; B0_hi ; B1_hi]
+//   A rows: [cos, sin](phase_A);  static B rows (192):  [B0_lo ; B0_hi ; B1_hi], each block of 64
+//       rows in groups of four (re y, re y+1, im y, im y+1), y even, so that the epilogue reads
+//       rows y and y + 1 as packed FP32 pairs
 //   MMA1: A_hi x B rows 64-191 (N128) -> cols 0..127 = [T0 | T1];  MMA2: A_hi x B0_lo (N64),
 //   MMA3: A_lo x B0_hi (N64) -> cols 0..63.  Two accumulators alternate (256 columns).
 
@@ -410,11 +412,11 @@ __global__ void __launch_bounds__(kGThreads, 2)
         // stores each operand row group as one 16-byte line of an MN-major core matrix
         // (8 rows of one k): a warp writes 512 contiguous bytes per row group.
         const int half = warp & 1, rg = warp >> 1, kl = 32 * half + lane;
-        float mt[8], gt[8];  // m_y and g_y of the 8 rows (l_x and f_x are the same values)
+        float2 mt[4], gt[4];  // m_y and g_y of the 8 rows in pairs (l_x and f_x are the same values)
 #pragma unroll
-        for (int j = 0; j < 8; j++) {
-            mt[j] = a.lmn[8 * rg + j];
-            gt[j] = a.tabs[8 * rg + j];
+        for (int j = 0; j < 4; j++) {
+            mt[j] = make_float2(a.lmn[8 * rg + 2 * j], a.lmn[8 * rg + 2 * j + 1]);
+            gt[j] = make_float2(a.tabs[8 * rg + 2 * j], a.tabs[8 * rg + 2 * j + 1]);
         }
         float sv = 1.f;  // FP16: power-of-two scale of this item's visibilities
         if (!BF16) {
@@ -456,27 +458,30 @@ __global__ void __launch_bounds__(kGThreads, 2)
             // 7.8e-6 total error measured there against 7.7e-6 with FP32 products; 2.9 % faster)
             const uint32_t dw2 = Half16<BF16>::pack(dws, dws);
             const float vre = vv.x * sv, vim = vv.y * sv;
+            const float2 cx2 = make_float2(c.x, c.x), cy2 = make_float2(c.y, c.y), cz2 = make_float2(c.z, c.z);
+            const float2 vre2 = make_float2(vre, vre), vim2 = make_float2(vim, vim), nvim2 = make_float2(-vim, -vim);
+            const float2 dws2 = make_float2(dws, dws);
             // words: [row pair][type] with type = Bh_re, Bh_im, B1_re, B1_im, Bl_re, Bl_im, Wh_re, Wh_im,
             // Wl_re, Wl_im; a pair packs rows (2p, 2p+1) of the warp's eight
             uint32_t wd[4][O2 ? 12 : 10];
 #pragma unroll
             for (int pr = 0; pr < 4; pr++) {
-                float cb[2], sb[2], wre[2], wim[2];
-#pragma unroll
-                for (int u = 0; u < 2; u++) {
-                    const int j = 2 * pr + u;
-                    const float zg = c.z * gt[j];
-                    __sincosf(fmaf(c.y, mt[j], zg), &sb[u], &cb[u]);  // B_k(y)
-                    float sa, ca;
-                    __sincosf(fmaf(c.x, mt[j], zg), &sa, &ca);       // A_k(x)
-                    wre[u] = vre * ca - vim * sa;
-                    wim[u] = vre * sa + vim * ca;
-                }
-                split_pair<BF16>(cb[0], cb[1], wd[pr][0], wd[pr][4]);
-                split_pair<BF16>(sb[0], sb[1], wd[pr][1], wd[pr][5]);
+                // the two rows of a pair side by side in packed FP32x2 arithmetic
+                const float2 zg = __fmul2_rn(cz2, gt[pr]);
+                const float2 pb = __ffma2_rn(cy2, mt[pr], zg), pa = __ffma2_rn(cx2, mt[pr], zg);
+                float2 cb, sb, ca, sa;
+                __sincosf(pb.x, &sb.x, &cb.x);  // B_k(y)
+                __sincosf(pb.y, &sb.y, &cb.y);
+                __sincosf(pa.x, &sa.x, &ca.x);  // A_k(x)
+                __sincosf(pa.y, &sa.y, &ca.y);
+                const float2 wre = __ffma2_rn(vre2, ca, __fmul2_rn(nvim2, sa));
+                const float2 wim = __ffma2_rn(vre2, sa, __fmul2_rn(vim2, ca));
+                split_pair<BF16>(cb.x, cb.y, wd[pr][0], wd[pr][4]);
+                split_pair<BF16>(sb.x, sb.y, wd[pr][1], wd[pr][5]);
                 if (O2) {  // dw * B rounded once from FP32: the first-order term reaches 0.03 here
-                    wd[pr][2] = Half16<BF16>::pack(dws * cb[0], dws * cb[1]);
-                    wd[pr][3] = Half16<BF16>::pack(dws * sb[0], dws * sb[1]);
+                    const float2 dcb = __fmul2_rn(dws2, cb), dsb = __fmul2_rn(dws2, sb);
+                    wd[pr][2] = Half16<BF16>::pack(dcb.x, dcb.y);
+                    wd[pr][3] = Half16<BF16>::pack(dsb.x, dsb.y);
                 } else {
                     wd[pr][2] = Half16<BF16>::mul2(wd[pr][0], dw2);  // dw * Bh (hi only)
                     wd[pr][3] = Half16<BF16>::mul2(wd[pr][1], dw2);
@@ -485,8 +490,8 @@ __global__ void __launch_bounds__(kGThreads, 2)
                     wd[pr][O2 ? 10 : 0] = Half16<BF16>::mul2(wd[pr][2], dw2);  // dw^2 * Bh
                     wd[pr][O2 ? 11 : 1] = Half16<BF16>::mul2(wd[pr][3], dw2);
                 }
-                split_pair<BF16>(wre[0], wre[1], wd[pr][6], wd[pr][8]);
-                split_pair<BF16>(wim[0], wim[1], wd[pr][7], wd[pr][9]);
+                split_pair<BF16>(wre.x, wre.y, wd[pr][6], wd[pr][8]);
+                split_pair<BF16>(wim.x, wim.y, wd[pr][7], wd[pr][9]);
             }
             // MN-major: row group G (8 rows) of an operand at G * 1024 bytes, k at 16 k
             const uint32_t A = sbase + s * kGStageBytes, B = A + kGStageA;
@@ -659,7 +664,7 @@ __global__ void __launch_bounds__(kDThreads, 2)
         tmem_alloc(tmem_slot, kDTmemCols);
         tmem_relinquish();
     }
-    // static B operand from the subgrid: rows (block, 2y+p), k = 2x + q
+    // static B operand from the subgrid: row (block, 4 (y / 2) + 2 p + y % 2), k = 2x + q
     float sq = 1.f;  // FP16: power-of-two scale of this subgrid's pixels
     if (warp < 8) {
         const float2 *data = a.subgrids + static_cast<int64_t>(it.subgrid) * kS * kS;
@@ -678,7 +683,7 @@ __global__ void __launch_bounds__(kDThreads, 2)
         for (int cc = threadIdx.x; cc < (O2 ? 256 : 192) * 8; cc += 256) {
             const int cm = cc >> 3, r8 = cc & 7;
             const int row = (cm >> 3) * 8 + r8, kg = cm & 7;
-            const int blk = row >> 6, rr = row & 63, y = rr >> 1, p = rr & 1;
+            const int blk = row >> 6, rr = row & 63, y = ((rr >> 2) << 1) | (rr & 1), p = (rr >> 1) & 1;
             uint32_t w[4];
 #pragma unroll
             for (int u = 0; u < 4; u++) {
@@ -800,11 +805,11 @@ __global__ void __launch_bounds__(kDThreads, 2)
         // (u < 8): rows 8 (2u + t/64) + t%8 = row0 + 16 u, one fixed group of 4 x values.
         const int kg = (threadIdx.x >> 3) & 7;
         const int row0 = (threadIdx.x >> 6) * 8 + (threadIdx.x & 7);
-        float lx[4], fx[4];
+        float2 lx[2], fx[2];  // l_x and f_x of the thread's 4 x values, in pairs
 #pragma unroll
-        for (int v = 0; v < 4; v++) {
-            lx[v] = tab_m[kg * 4 + v];
-            fx[v] = tab_g[kg * 4 + v];
+        for (int v = 0; v < 2; v++) {
+            lx[v] = make_float2(tab_m[kg * 4 + 2 * v], tab_m[kg * 4 + 2 * v + 1]);
+            fx[v] = make_float2(tab_g[kg * 4 + 2 * v], tab_g[kg * 4 + 2 * v + 1]);
         }
         for (int i = 0; i < ntiles; i++) {
             const int b = i & 1, slot = i % kDRing;
@@ -838,11 +843,15 @@ __global__ void __launch_bounds__(kDThreads, 2)
             for (int u = 0; u < 8; u++) {
                 const int cc = threadIdx.x + 128 * u;
                 uint32_t whi[4], wlo[4];
+                const float2 cx = make_float2(cu[u].x, cu[u].x), cz = make_float2(cu[u].y, cu[u].y);
 #pragma unroll
-                for (int v = 0; v < 4; v++) {
+                for (int v = 0; v < 2; v++) {
+                    const float2 ph = __ffma2_rn(cx, lx[v], __fmul2_rn(cz, fx[v]));
                     float sa, ca;
-                    __sincosf(fmaf(cu[u].x, lx[v], cu[u].y * fx[v]), &sa, &ca);
-                    split_pair<BF16, !BF16>(ca, sa, whi[v], wlo[v]);
+                    __sincosf(ph.x, &sa, &ca);
+                    split_pair<BF16, !BF16>(ca, sa, whi[2 * v], wlo[2 * v]);
+                    __sincosf(ph.y, &sa, &ca);
+                    split_pair<BF16, !BF16>(ca, sa, whi[2 * v + 1], wlo[2 * v + 1]);
                 }
                 st_shared_v4(ahi + cc * 16, whi[0], whi[1], whi[2], whi[3]);
                 st_shared_v4(alo + cc * 16, wlo[0], wlo[1], wlo[2], wlo[3]);
@@ -881,10 +890,29 @@ __global__ void __launch_bounds__(kDThreads, 2)
             tc_fence_after();
             const float dwe = BF16 ? c.z : c.z / a.r_scale;  // T1 was formed from r * r_scale
             const uint32_t acc = tmem + (static_cast<uint32_t>(32 * q) << 16) + static_cast<uint32_t>(b * 128);
-            float vre[2] = {0.f, 0.f}, vim[2] = {0.f, 0.f};  // even and odd rows: two independent chains
+            // accumulator columns come in groups of four: (re y, re y+1, im y, im y+1), so rows y and
+            // y + 1 are handled side by side in packed FP32x2 arithmetic; vis = sum over y of
+            // conj(B) z = (a1 + a2) + i (a3 - a4), both halves of each pair summed at the end
+            const float2 cy = make_float2(c.y, c.y), cz = make_float2(c.z, c.z);
+            const float2 dw = make_float2(dwe, dwe), ndw = make_float2(-dwe, -dwe);
+            float2 a1 = make_float2(0.f, 0.f), a2 = a1, a3 = a1, a4 = a1;
+            auto row_pair = [&](int y0, float2 zre, float2 zim) {
+                const float2 my = BATCH ? make_float2(tab_m[y0], tab_m[y0 + 1]) : make_float2(L.m_tab[y0], L.m_tab[y0 + 1]);
+                const float2 gy = BATCH ? make_float2(tab_g[y0], tab_g[y0 + 1]) : make_float2(L.g_tab[y0], L.g_tab[y0 + 1]);
+                const float2 ph = __ffma2_rn(cy, my, __fmul2_rn(cz, gy));
+                float2 sb, cb;
+                __sincosf(ph.x, &sb.x, &cb.x);
+                __sincosf(ph.y, &sb.y, &cb.y);
+                a1 = __ffma2_rn(cb, zre, a1);
+                a2 = __ffma2_rn(sb, zim, a2);
+                a3 = __ffma2_rn(cb, zim, a3);
+                a4 = __ffma2_rn(sb, zre, a4);
+            };
+            auto pair = [](const uint32_t *t, int i) { return make_float2(__uint_as_float(t[i]), __uint_as_float(t[i + 1])); };
             if (O2) {
                 // z = T0 - i dw T1 - (dw^2 / 2) T2, 8 rows (16 columns) of each block at a time
                 const float hd2 = 0.5f * dwe * dwe;  // T2 was formed from r^2 * r_scale^2
+                const float2 nhd2 = make_float2(-hd2, -hd2);
 #pragma unroll
                 for (int h = 0; h < 4; h++) {
                     uint32_t t0[16], t1[16], t2[16];
@@ -895,42 +923,29 @@ __global__ void __launch_bounds__(kDThreads, 2)
                     tmem_ld_wait(t1);
                     tmem_ld_wait(t2);
 #pragma unroll
-                    for (int yy = 0; yy < 8; yy++) {
-                        const int y = h * 8 + yy;
-                        const float t0re = __uint_as_float(t0[2 * yy]), t0im = __uint_as_float(t0[2 * yy + 1]);
-                        const float t1re = __uint_as_float(t1[2 * yy]), t1im = __uint_as_float(t1[2 * yy + 1]);
-                        const float t2re = __uint_as_float(t2[2 * yy]), t2im = __uint_as_float(t2[2 * yy + 1]);
-                        const float zre = fmaf(-hd2, t2re, fmaf(dwe, t1im, t0re));
-                        const float zim = fmaf(-hd2, t2im, fmaf(-dwe, t1re, t0im));
-                        float sb, cb;
-                        const float my = BATCH ? tab_m[y] : L.m_tab[y], gy = BATCH ? tab_g[y] : L.g_tab[y];
-                        __sincosf(fmaf(c.y, my, c.z * gy), &sb, &cb);
-                        vre[yy & 1] = fmaf(cb, zre, fmaf(sb, zim, vre[yy & 1]));
-                        vim[yy & 1] = fmaf(cb, zim, fmaf(-sb, zre, vim[yy & 1]));
+                    for (int yq = 0; yq < 4; yq++) {
+                        const float2 zre = __ffma2_rn(nhd2, pair(t2, 4 * yq), __ffma2_rn(dw, pair(t1, 4 * yq + 2), pair(t0, 4 * yq)));
+                        const float2 zim = __ffma2_rn(nhd2, pair(t2, 4 * yq + 2), __ffma2_rn(ndw, pair(t1, 4 * yq), pair(t0, 4 * yq + 2)));
+                        row_pair(h * 8 + 2 * yq, zre, zim);
                     }
                 }
             }
 #pragma unroll
-            for (int h = 0; h < (O2 ? 0 : 2); h++) {
-                uint32_t t0[32], t1[32];
-                tmem_ld32(acc + h * 32, t0);
-                tmem_ld32(acc + 64 + h * 32, t1);
+            for (int h = 0; h < (O2 ? 0 : 4); h++) {
+                uint32_t t0[16], t1[16];
+                tmem_ld16(acc + h * 16, t0);
+                tmem_ld16(acc + 64 + h * 16, t1);
                 tmem_ld_wait(t0);
                 tmem_ld_wait(t1);
 #pragma unroll
-                for (int yy = 0; yy < 16; yy++) {
-                    const int y = h * 16 + yy;
-                    const float t0re = __uint_as_float(t0[2 * yy]), t0im = __uint_as_float(t0[2 * yy + 1]);
-                    const float t1re = __uint_as_float(t1[2 * yy]), t1im = __uint_as_float(t1[2 * yy + 1]);
-                    const float zre = fmaf(dwe, t1im, t0re), zim = fmaf(-dwe, t1re, t0im);
-                    float sb, cb;
-                    // single-plan launches: the tables are kernel parameters (constant bank)
-                    const float my = BATCH ? tab_m[y] : L.m_tab[y], gy = BATCH ? tab_g[y] : L.g_tab[y];
-                    __sincosf(fmaf(c.y, my, c.z * gy), &sb, &cb);
-                    vre[yy & 1] = fmaf(cb, zre, fmaf(sb, zim, vre[yy & 1]));
-                    vim[yy & 1] = fmaf(cb, zim, fmaf(-sb, zre, vim[yy & 1]));
+                for (int yq = 0; yq < 4; yq++) {
+                    // z = T0 - i dw T1 (single-plan launches: the tables are kernel parameters)
+                    const float2 zre = __ffma2_rn(dw, pair(t1, 4 * yq + 2), pair(t0, 4 * yq));
+                    const float2 zim = __ffma2_rn(ndw, pair(t1, 4 * yq), pair(t0, 4 * yq + 2));
+                    row_pair(h * 8 + 2 * yq, zre, zim);
                 }
             }
+            const float vre_s = (a1.x + a1.y) + (a2.x + a2.y), vim_s = (a3.x + a3.y) - (a4.x + a4.y);
             tc_fence_before();
             __syncwarp();
             if (lane == 0) {
@@ -939,7 +954,7 @@ __global__ void __launch_bounds__(kDThreads, 2)
             }
             if (j < nvis) {
                 const float sc = g.inv_s2 / sq;  // exact: sq is a power of two
-                store_vis(out, j, make_float2((vre[0] + vre[1]) * sc, (vim[0] + vim[1]) * sc));
+                store_vis(out, j, make_float2(vre_s * sc, vim_s * sc));
             }
         }
     }
