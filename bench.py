@@ -678,7 +678,8 @@ def main():
     plan = part.plan
     info = plan.info()
     headline = "tc_bf16x3" if args.mode == "auto" else args.mode
-    compare = ["fp32"] if args.mode == "auto" else []
+    # config 3 times both split-precision forms beside the FP32 kernels
+    compare = ["fp32", "tc_fp16x3"] if args.mode == "auto" else []
 
     stream = torch.cuda.Stream()
     plan.set_stream(stream.cuda_stream)

@@ -44,7 +44,9 @@ enum {
     P9IDG_DEVICE_CHECK_FAILED = 9   /* a kernel's own bounds check tripped (no access was made) */
 };
 
-/* Gridding precision of the gridder/degridder kernels. */
+/* Gridding precision of the gridder/degridder kernels.  The FP32 kernels take subgrid sizes 8, 16,
+ * 24, 32 and 48; the tensor-core kernels 8, 16, 24 and 32 (a subgrid of S < 32 runs padded to 32
+ * operand rows, so it costs what S = 32 costs per visibility). */
 enum {
     P9IDG_MODE_FP32 = 0,      /* FP32 sincos + FMA, FP64 per-visibility phase argument */
     P9IDG_MODE_TC_BF16X3 = 1, /* tensor cores, BF16 hi+lo split (3 products), FP32 accumulation */
@@ -234,7 +236,7 @@ p9idg_status p9idg_grid_w_device_noalloc(const p9idg_params *c, const p9idg_subg
  * small problems fill the GPU alongside large ones.  Buffers are the per-problem device
  * buffers of p9idg_grid_w_device / p9idg_degrid_w_device (complex64), fixed at creation.
  * All plans must share the precision mode; FP32 batches may mix subgrid sizes (one launch per
- * kernel stage and size), tensor-core batches use S = 32 throughout. */
+ * kernel stage and size), tensor-core batches use one subgrid size throughout. */
 typedef struct p9idg_batch p9idg_batch;
 
 /* Work-item sizes (visibilities per gridder / degridder item; 0 = default) -- the time-chunk

@@ -54,7 +54,10 @@ namespace {
 
 using namespace tc;
 
-constexpr int kS = 32;
+constexpr int kS = 32;  // operand rows per subgrid axis: a subgrid of S < 32 pixels is padded to 32
+// plan tables (device floats), each padded with zeros past the plan's S: the separable part g[32],
+// the remainder r[32][32], and l[32] (the reference's FP32 ComputeL values)
+constexpr int kTabR = kS, kTabL = kS + kS * kS, kTabs = kTabL + kS;
 constexpr uint64_t kWaitNs = 2000000000ull;  // 2 s per wait before a kernel gives up
 
 // Tensor maps for TMA staging (single-plan launches with complex64 visibilities in device
@@ -65,6 +68,12 @@ struct TmaMaps {
     CUtensorMap vis;
 };
 constexpr int kVisBox = 66;
+
+// (i + S / 2) mod S for 0 <= i < S: the fftshifted index of a subgrid pixel, without a division
+__device__ __forceinline__ int shift_half(int i, int S) {
+    const int j = i + (S >> 1);
+    return j >= S ? j - S : j;
+}
 
 // The dynamic shared memory rounded up to a 1 KB boundary by pointer arithmetic on the
 // __shared__ array itself, so that every pointer derived from it stays in the shared state
@@ -228,6 +237,45 @@ static_assert(kGEpilogue <= kGStages * kGStageBytes, "epilogue planes must fit i
 constexpr uint32_t kGSmem = kGStages * kGStageBytes + kGRing * kGRingSlot + 512 + 1024;
 constexpr uint32_t kGTmemCols = 128;   // first order: [Wh | Wl] against the A rows of MMA1 (MMA2 adds in)
 constexpr uint32_t kGTmemCols2 = 256;  // second order: MMA2 (Bl and B2 rows) into its own columns 128-191
+
+// The gridder epilogue's last step for the 4 pixels a producer thread finishes: P = P0 + i r P1
+// (- (r^2 / 2) P2) from the planes E, times the taper, into the work item's partial subgrid
+// (fftshifted as Gridder.Forward writes it).  Rows and columns past the plan's S are padding:
+// computed, never written.  SC: the subgrid size when it is the full 32 (compile-time indexing),
+// else 0 and s_rt.
+template <int SC, bool O2>
+__device__ __forceinline__ void gridder_finish(const TcArgs &a, const float *E, int s_rt, int slot, float sv,
+                                               float sw) {
+    const int S = SC ? SC : s_rt;
+    float ep_r[4], ep_t[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const int p = threadIdx.x + k * kGProducerWarps * 32;
+        const int y = p >> 5, x = p & 31;
+        ep_r[k] = a.tabs[kTabR + p];
+        ep_t[k] = (y < S && x < S) ? a.taper[y * S + x] : 0.f;
+    }
+    float2 *out = a.partials + static_cast<int64_t>(slot) * S * S;
+    const float i0 = 1.f / sv, i1 = 1.f / (sv * sw), i2 = 0.5f / (sv * sw * sw);  // exact: powers of two
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const int p = threadIdx.x + k * kGProducerWarps * 32;
+        const int y = p >> 5, x = p & 31;
+        const int e = y * 33 + x;
+        const float p0re = (E[0 * 1056 + e] - E[3 * 1056 + e]) * i0;
+        const float p0im = (E[1 * 1056 + e] + E[2 * 1056 + e]) * i0;
+        const float p1re = (E[4 * 1056 + e] - E[7 * 1056 + e]) * i1;
+        const float p1im = (E[5 * 1056 + e] + E[6 * 1056 + e]) * i1;
+        const float rr = ep_r[k], tap = ep_t[k];
+        float re = fmaf(-rr, p1im, p0re), im = fmaf(rr, p1re, p0im);
+        if (O2) {  // - (r^2 / 2) P2
+            const float h2 = rr * rr * i2;
+            re = fmaf(-h2, E[8 * 1056 + e] - E[11 * 1056 + e], re);
+            im = fmaf(-h2, E[9 * 1056 + e] + E[10 * 1056 + e], im);
+        }
+        if (y < S && x < S) out[shift_half(y, S) * S + shift_half(x, S)] = make_float2(re * tap, im * tap);
+    }
+}
 
 // O2: the second-order form (|dw r| up to P9IDG_TC_MAX_W_TERM2): rows 192-255 of the A operand,
 // zero in the first-order form, carry B2 = dw^2 Bh, and MMA2 accumulates into its own columns, so
@@ -415,7 +463,7 @@ __global__ void __launch_bounds__(kGThreads, 2)
         float2 mt[4], gt[4];  // m_y and g_y of the 8 rows in pairs (l_x and f_x are the same values)
 #pragma unroll
         for (int j = 0; j < 4; j++) {
-            mt[j] = make_float2(a.lmn[8 * rg + 2 * j], a.lmn[8 * rg + 2 * j + 1]);
+            mt[j] = make_float2(a.tabs[kTabL + 8 * rg + 2 * j], a.tabs[kTabL + 8 * rg + 2 * j + 1]);
             gt[j] = make_float2(a.tabs[8 * rg + 2 * j], a.tabs[8 * rg + 2 * j + 1]);
         }
         float sv = 1.f;  // FP16: power-of-two scale of this item's visibilities
@@ -550,33 +598,10 @@ __global__ void __launch_bounds__(kGThreads, 2)
         tc_fence_before();
         named_bar(1, kGProducerWarps * 32);
         if (ok && !*abort_flag) {
-            float ep_r[4], ep_t[4];  // remainder r and taper of the 4 pixels this thread finishes
-#pragma unroll
-            for (int k = 0; k < 4; k++) {
-                const int p = threadIdx.x + k * kGProducerWarps * 32;
-                ep_r[k] = a.tabs[kS + p];
-                ep_t[k] = a.taper[p];
-            }
-            float2 *out = a.partials + static_cast<int64_t>(it.slot) * kS * kS;
-            const float i0 = 1.f / sv, i1 = 1.f / (sv * sw), i2 = 0.5f / (sv * sw * sw);  // exact: powers of two
-#pragma unroll
-            for (int k = 0; k < 4; k++) {
-                const int p = threadIdx.x + k * kGProducerWarps * 32;
-                const int y = p >> 5, x = p & 31;
-                const int e = y * 33 + x;
-                const float p0re = (E[0 * 1056 + e] - E[3 * 1056 + e]) * i0;
-                const float p0im = (E[1 * 1056 + e] + E[2 * 1056 + e]) * i0;
-                const float p1re = (E[4 * 1056 + e] - E[7 * 1056 + e]) * i1;
-                const float p1im = (E[5 * 1056 + e] + E[6 * 1056 + e]) * i1;
-                const float rr = ep_r[k], tap = ep_t[k];
-                float re = fmaf(-rr, p1im, p0re), im = fmaf(rr, p1re, p0im);
-                if (O2) {  // - (r^2 / 2) P2
-                    const float h2 = rr * rr * i2;
-                    re = fmaf(-h2, E[8 * 1056 + e] - E[11 * 1056 + e], re);
-                    im = fmaf(-h2, E[9 * 1056 + e] + E[10 * 1056 + e], im);
-                }
-                out[((y + kS / 2) % kS) * kS + (x + kS / 2) % kS] = make_float2(re * tap, im * tap);
-            }
+            if (g.S == kS)  // the full size with compile-time indexing, smaller subgrids padded
+                gridder_finish<kS, O2>(a, E, g.S, it.slot, sv, sw);
+            else
+                gridder_finish<0, O2>(a, E, g.S, it.slot, sv, sw);
         }
     }
     tc_fence_before();
@@ -657,24 +682,28 @@ __global__ void __launch_bounds__(kDThreads, 2)
         mbar_fence_init();
     }
     if (threadIdx.x < kS) {
-        tab_m[threadIdx.x] = a.lmn[threadIdx.x];
+        tab_m[threadIdx.x] = a.tabs[kTabL + threadIdx.x];
         tab_g[threadIdx.x] = a.tabs[threadIdx.x];
     }
     if (warp == kDMmaWarp) {
         tmem_alloc(tmem_slot, kDTmemCols);
         tmem_relinquish();
     }
-    // static B operand from the subgrid: row (block, 4 (y / 2) + 2 p + y % 2), k = 2x + q
+    // static B operand from the subgrid: row (block, 4 (y / 2) + 2 p + y % 2), k = 2x + q; pixels
+    // past the plan's S (a subgrid of S < 32 padded to 32) are zero
     float sq = 1.f;  // FP16: power-of-two scale of this subgrid's pixels
     if (warp < 8) {
-        const float2 *data = a.subgrids + static_cast<int64_t>(it.subgrid) * kS * kS;
+        const int S = g.S;
+        const float2 *data = a.subgrids + static_cast<int64_t>(it.subgrid) * S * S;
         if (!BF16) {
             float mx = 0.f;
             for (int pi = threadIdx.x; pi < kS * kS; pi += 256) {
                 const int y = pi >> 5, x = pi & 31;
-                const float2 d = data[((y + kS / 2) % kS) * kS + (x + kS / 2) % kS];
-                const float tap = fabsf(a.taper[pi]);
-                mx = fmaxf(mx, fmaxf(fabsf(d.x), fabsf(d.y)) * tap);
+                if (y < S && x < S) {
+                    const float2 d = data[shift_half(y, S) * S + shift_half(x, S)];
+                    const float tap = fabsf(a.taper[y * S + x]);
+                    mx = fmaxf(mx, fmaxf(fabsf(d.x), fabsf(d.y)) * tap);
+                }
             }
             sq = pow2_scale(block256_max(mx, red));
         }
@@ -684,16 +713,35 @@ __global__ void __launch_bounds__(kDThreads, 2)
             const int cm = cc >> 3, r8 = cc & 7;
             const int row = (cm >> 3) * 8 + r8, kg = cm & 7;
             const int blk = row >> 6, rr = row & 63, y = ((rr >> 2) << 1) | (rr & 1), p = (rr >> 1) & 1;
+            // the four x of this chunk: S is a multiple of 4, so they are wholly inside or outside the
+            // subgrid and on one side of the fftshift wrap (consecutive source pixels)
+            const int x0 = kg * 4;
+            float2 dv[4];
+            float tv[4];
+            if (y < S && x0 < S) {
+                const float2 *src = data + shift_half(y, S) * S + shift_half(x0, S);
+                const float *tsrc = a.taper + y * S + x0;
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    dv[u] = src[u];
+                    tv[u] = tsrc[u] * sq;
+                }
+            } else {
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    dv[u] = make_float2(0.f, 0.f);
+                    tv[u] = 0.f;
+                }
+            }
             uint32_t w[4];
 #pragma unroll
             for (int u = 0; u < 4; u++) {
-                const int x = kg * 4 + u;
-                const int pi = y * kS + x;
-                const float2 d = data[((y + kS / 2) % kS) * kS + (x + kS / 2) % kS];
-                const float tap = a.taper[pi] * sq;
+                const int x = x0 + u;
+                const float2 d = dv[u];
+                const float tap = tv[u];
                 float qre = tap * d.x, qim = tap * d.y;
                 if (blk >= 2) {  // r (.) pix, and r^2 (.) pix for block 3
-                    const float rr2 = a.tabs[kS + pi] * sr;
+                    const float rr2 = a.tabs[kTabR + y * kS + x] * sr;
                     qre *= rr2;
                     qim *= rr2;
                     if (blk == 3) {
@@ -1083,7 +1131,8 @@ void fill_args(TcArgs &t, const GridderArgs &a, const TcPlanState &st) {
 
 }  // namespace
 
-bool tc_subgrid_size_supported(int S) { return S == kS; }
+// S < 32 runs padded to 32 operand rows (the per-visibility cost of S = 32)
+bool tc_subgrid_size_supported(int S) { return S == 8 || S == 16 || S == 24 || S == 32; }
 
 int tc_order_for(double w_term, int want_order) {
     if (want_order != 2 && w_term <= P9IDG_TC_MAX_W_TERM) return 1;
@@ -1105,15 +1154,17 @@ void tc_debug_set(uint64_t wait_ns, int32_t skip_stage) {
 
 namespace {
 
-// The separable part f (S floats, serving as f(x) and g(y)) and the remainder r (S*S floats) of
-// the reference's FP32 n table (Gridder.cs:168-174 values in lmn[S..]): f(x) = n(l_x, 0) + c/2
-// and r = n - f(x) - f(y), where the constant c centres the range of r on zero.  Returns max |r|.
+// The separable part f (serving as f(x) and g(y)) and the remainder r of the reference's FP32 n
+// table (Gridder.cs:168-174 values in lmn[S..]): f(x) = n(l_x, 0) + c/2 and r = n - f(x) - f(y),
+// where the constant c centres the range of r on zero; with l (lmn[0..S)) they make the kTabs-float
+// table the kernels read, padded with zeros past S.  Returns max |r| over the S x S pixels.
 double separable_tables(const std::vector<float> &lmn, int S, std::vector<float> &tabs) {
-    tabs.assign(S + S * S, 0.f);
+    tabs.assign(kTabs, 0.f);
     std::vector<double> f0(S);
     for (int x = 0; x < S; x++) {
         const double l = lmn[x], t = l * l;
         f0[x] = t / (t + std::sqrt(1.0 - t));
+        tabs[kTabL + x] = lmn[x];
     }
     double rlo = INFINITY, rhi = -INFINITY;
     for (int y = 0; y < S; y++)
@@ -1129,7 +1180,7 @@ double separable_tables(const std::vector<float> &lmn, int S, std::vector<float>
     for (int y = 0; y < S; y++)
         for (int x = 0; x < S; x++) {
             const double r = static_cast<double>(lmn[S + y * S + x]) - tabs[x] - tabs[y];
-            tabs[S + y * S + x] = static_cast<float>(r);
+            tabs[kTabR + y * kS + x] = static_cast<float>(r);
             rmax = std::max(rmax, std::fabs(r));
         }
     return rmax;
@@ -1152,7 +1203,7 @@ void w_k_max(const std::vector<p9idg_subgrid> &subs, const std::vector<double> &
 
 double tc_w_term(const std::vector<p9idg_subgrid> &subs, const std::vector<float> &lmn, int S,
                  const std::vector<double> &wn, const double *uvw_host, int nt_all) {
-    if (S != kS) return INFINITY;
+    if (!tc_subgrid_size_supported(S)) return INFINITY;
     std::vector<float> tabs;
     const double rmax = separable_tables(lmn, S, tabs);
     double wmax, kmax;
@@ -1164,8 +1215,8 @@ p9idg_status tc_prepare(TcPlanState &st, const std::vector<p9idg_subgrid> &subs,
                         int S, int nch, const std::vector<double> &wn, const double *uvw_host, int nt_all,
                         cudaStream_t stream, std::string &err) {
     if (st.ready) return P9IDG_OK;
-    if (S != kS) {
-        err = "tensor-core kernels support subgrid size 32 only";
+    if (!tc_subgrid_size_supported(S)) {
+        err = "tensor-core kernels support subgrid sizes 8, 16, 24 and 32";
         return P9IDG_UNSUPPORTED;
     }
     std::vector<float> tabs;
@@ -1179,8 +1230,8 @@ p9idg_status tc_prepare(TcPlanState &st, const std::vector<p9idg_subgrid> &subs,
     st.max_w_r = wmax * kmax * rmax;
     st.r_max = rmax;
     tc_set_order(st, st.want_order);
-    for (int i = 0; i < S; i++) {
-        st.m_tab[i] = lmn[i];
+    for (int i = 0; i < kS; i++) {
+        st.m_tab[i] = tabs[kTabL + i];
         st.g_tab[i] = tabs[i];
     }
     // powers of two keeping dw * B and r * pix inside the FP16 range (|woff| = 0, so |dw| <= k |w|)

@@ -19,7 +19,8 @@ struct TcPlanState {
     int64_t ncoef = 0;
     void *coef = nullptr;         // float4 {du, dv, dw, 0} per gridded visibility, subgrid order
     void *coef_off = nullptr;     // int64 per subgrid: first coefficient of the subgrid
-    void *tables = nullptr;       // float: f[S] (separable part of n), r[S*S] (remainder)
+    void *tables = nullptr;       // float: g[32] (separable part of n), r[32][32] (remainder), l[32],
+                                  // zero past the plan's S
     void *ditems = nullptr;       // degridder work items (<= degrid_chunk visibilities)
     int32_t nditems = 0;
     std::vector<WorkItem> ditems_host;  // the same list on the host (batches merge them)

@@ -71,11 +71,33 @@ def test_tc_non_w_and_psf(need_gpu):
 
 def test_tc_rejects_other_subgrid_sizes():
     obs, cd = workload("small_256", n_ant=4, nt=50, nch=4)
-    c, cd = constants(cd, subgrid_size=16, kernel_size=4)
+    c, cd = constants(cd, subgrid_size=48, kernel_size=8)
     part = pkg.Partitioner.CreatePartition(c, obs.uvw, obs.frequencies)
     with pytest.raises(pkg.P9IDGError) as e:
         part.plan.set_mode(pkg.MODE_TC_BF16X3)
     assert e.value.code == 8
+
+
+@pytest.mark.parametrize("mode", MODES)
+@pytest.mark.parametrize("S", [8, 16, 24])
+def test_tc_smaller_subgrids(need_gpu, mode, S):
+    """Subgrids of S < 32 pixels run padded to the kernels' 32 operand rows (the padding rows and
+    columns are computed and never written, the padded pixels of the degridder's input are zero):
+    the same bound as S = 32 for w layers, degridded visibilities and the dirty image."""
+    obs, cd = workload("small_256", n_ant=8, nt=300, nch=8)
+    c, cd = constants(cd, subgrid_size=S, kernel_size=max(2, S // 4))
+    part = pkg.Partitioner.CreatePartition(c, obs.uvw, obs.frequencies)
+    assert part.plan.set_mode(mode) == mode
+    subs = oracle.partition(cd, obs.uvw, obs.frequencies)
+    got = pkg.IDG.GridW(c, part, obs.vis, obs.uvw, obs.frequencies)
+    ref = oracle.idg_grid_w(cd, subs, obs.vis, obs.uvw, obs.frequencies)
+    assert rel_l2(got, ref) < TOL_TC
+    img = pkg.FFT.WStackIFFTFloat(got, cd["vis_count"])
+    assert rel_l2(img, oracle.wstack_ifft_float(ref, cd["vis_count"])) < TOL_TC
+    model = oracle.fft_forward_float(oracle.shift(obs.model_image.astype(np.float32)))
+    vis = pkg.IDG.DeGridW(c, part, model.copy(), obs.uvw, obs.frequencies)
+    vref, _ = oracle.idg_degrid(cd, subs, model, obs.uvw, obs.frequencies, wstack=True)
+    assert rel_l2(vis, vref) < TOL_TC
 
 
 EDGE_SHAPES = [
