@@ -235,8 +235,8 @@ p9idg_status p9idg_grid_w_device_noalloc(const p9idg_params *c, const p9idg_subg
  * kernel stage is ONE launch over the work items of all problems, ordered largest first, so
  * small problems fill the GPU alongside large ones.  Buffers are the per-problem device
  * buffers of p9idg_grid_w_device / p9idg_degrid_w_device (complex64), fixed at creation.
- * All plans must share the precision mode; FP32 batches may mix subgrid sizes (one launch per
- * kernel stage and size), tensor-core batches use one subgrid size throughout. */
+ * All plans must share the precision mode; they may mix subgrid sizes (one launch per kernel
+ * stage and size). */
 typedef struct p9idg_batch p9idg_batch;
 
 /* Work-item sizes (visibilities per gridder / degridder item; 0 = default) -- the time-chunk

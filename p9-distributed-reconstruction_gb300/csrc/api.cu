@@ -947,13 +947,12 @@ struct p9idg_batch {
     std::vector<p9idg_plan *> plans;
     int device = -1;
     int32_t mode = P9IDG_MODE_FP32;
-    int32_t S = 0;
     cudaStream_t stream = nullptr;
     DevBuf d_gargs, d_dargs, d_aargs, d_sargs, d_tg, d_td;  // per-problem argument tables
     DevBuf d_gitems, d_ditems, d_refs, d_done_init, d_done, d_finish, d_start;
     int32_t ngitems = 0, nditems = 0, nrefs = 0;
     std::vector<WorkItem> h_gitems, h_ditems;  // merged work items of all problems, in launch order
-    // FP32 batches may mix subgrid sizes: the items and subgrid references are grouped by size,
+    // problems may mix subgrid sizes: the items and subgrid references are grouped by size,
     // one launch per kernel stage and size (group k: items [g0, g0 + gn), [d0, d0 + dn), refs [r0, r0 + rn))
     struct Group {
         int32_t S, g0, gn, d0, dn, r0, rn;
@@ -1564,8 +1563,6 @@ p9idg_status p9idg_batch_create(p9idg_plan *const *plans, int32_t nplans, const 
             return fail(P9IDG_INVALID_ARGUMENT, "null plan or buffer");
         if (plans[i]->mode != plans[0]->mode)
             return fail(P9IDG_UNSUPPORTED, "a batch needs one precision mode");
-        if (plans[i]->mode != P9IDG_MODE_FP32 && plans[i]->c.subgrid_size != plans[0]->c.subgrid_size)
-            return fail(P9IDG_UNSUPPORTED, "a tensor-core batch needs one subgrid size");
     }
     auto *b = new (std::nothrow) p9idg_batch();
     if (!b) return fail(P9IDG_OUT_OF_MEMORY, "batch allocation");
@@ -1576,7 +1573,6 @@ p9idg_status p9idg_batch_create(p9idg_plan *const *plans, int32_t nplans, const 
     };
     b->plans.assign(plans, plans + nplans);
     b->mode = plans[0]->mode;
-    b->S = plans[0]->c.subgrid_size;
     std::vector<GridderArgs> ga(nplans), da(nplans);
     std::vector<SubgridOpArgs> aa(nplans), sa(nplans);
     std::vector<TcArgs> tg(nplans), td(nplans);
