@@ -52,7 +52,7 @@ def _c128(a, name):
 
 
 def _f64(a):
-    return np.ascontiguousarray(a, dtype=np.float64)
+    return None if a is None else np.ascontiguousarray(a, dtype=np.float64)
 
 
 def _out(out, shape):
@@ -275,6 +275,12 @@ def plan_from_subgrids(c: GriddingConstants, subgrids: np.ndarray, uvw, frequenc
 
 
 def _plan_for(c: GriddingConstants, metadata, uvw, frequencies) -> Plan:
+    if uvw is None:
+        # the uvw the partition was made from, kept on the device by its plan (p9idg_* with uvw NULL)
+        if not (isinstance(metadata, Partition) and metadata.plan is not None
+                and metadata.plan.constants.key() == c.key() and metadata.plan.nch == len(frequencies)):
+            raise ValueError("uvw=None needs the Partition (with its plan) that Partitioner.CreatePartition made")
+        return metadata.plan
     uvw = np.asarray(uvw)
     if isinstance(metadata, Partition) and metadata.plan is not None:
         p = metadata.plan
@@ -326,7 +332,10 @@ class IDG:
     @staticmethod
     def GridW(c, metadata, visibilities, uvw, frequencies, out=None) -> np.ndarray:
         """`out` (optional): a C-contiguous complex128 [W][N][N] array to write into, e.g. in
-        page-locked memory; the reference returns a new List<Complex[,]>."""
+        page-locked memory; the reference returns a new List<Complex[,]>.  `uvw` None (here and in
+        every IDG member): the uvw the partition was made from, which its plan keeps on the device,
+        so a call uploads and compares none (the reference's callers pass the same uvw every
+        cycle, MajorCycle.cs:46,88)."""
         p = _plan_for(c, metadata, uvw, frequencies)
         vis, uvw = _c128(visibilities, "visibilities"), _f64(uvw)
         _check_inputs(p, c, vis=vis, uvw=uvw)

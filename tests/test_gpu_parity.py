@@ -159,6 +159,29 @@ def test_device_api_matches_host_api(need_gpu):
     plan.set_stream(0)
 
 
+@pytest.mark.parametrize("mode", [pkg.MODE_FP32, pkg.MODE_TC_BF16X3], ids=["fp32", "tc_bf16x3"])
+def test_uvw_kept_on_the_device(need_gpu, mode):
+    """uvw=None (NULL in the C ABI): the uvw the partition was made from, which the plan keeps on
+    the device.  The same results as passing it, also after a call with another uvw in between
+    (that call's uvw replaces the device copy; the next None call puts the plan's back)."""
+    obs, c, cd, part, subs = _setup("small_256", dict(n_ant=8, nt=300, nch=8))
+    assert part.plan.set_mode(mode) == mode
+    model = _model_grid(obs)
+    lay = pkg.IDG.GridW(c, part, obs.vis, obs.uvw, obs.frequencies)
+    vis = pkg.IDG.DeGridW(c, part, model.copy(), obs.uvw, obs.frequencies)
+    other = obs.uvw.copy()
+    other[..., 2] *= 0.5
+    tol = TOL if mode == pkg.MODE_FP32 else 1e-4
+    for step in range(2):
+        assert rel_l2(pkg.IDG.GridW(c, part, obs.vis, None, obs.frequencies), lay) < 1e-6
+        assert np.array_equal(pkg.IDG.DeGridW(c, part, model.copy(), None, obs.frequencies), vis)
+        lay_o = pkg.IDG.GridW(c, part, obs.vis, other, obs.frequencies)
+        assert rel_l2(lay_o, oracle.idg_grid_w(cd, subs, obs.vis, other, obs.frequencies)) < tol
+    assert rel_l2(lay, oracle.idg_grid_w(cd, subs, obs.vis, obs.uvw, obs.frequencies)) < tol
+    with pytest.raises(ValueError):
+        pkg.IDG.GridW(c, [list(x) for x in part], obs.vis, None, obs.frequencies)
+
+
 def test_adjoint_identity_gpu(need_gpu):
     obs, c, cd, part, subs = _setup("small_256", dict(n_ant=10, nt=400, nch=8))
     rng = np.random.default_rng(4)
