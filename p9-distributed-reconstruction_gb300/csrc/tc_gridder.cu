@@ -155,12 +155,6 @@ __device__ __forceinline__ void named_bar(int id, int nthreads) {
     asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
 }
 
-
-__device__ __forceinline__ void st_shared_v2(uint32_t addr, uint32_t a, uint32_t b) {
-    asm volatile("st.shared.v2.b32 [%0], {%1, %2};" ::"r"(addr), "r"(a), "r"(b) : "memory");
-}
-
-
 // 2^-e with m * 2^-e in [0.5, 1) (1 for m == 0): exact power-of-two scale
 __device__ __forceinline__ float pow2_scale(float m) {
     if (!(m > 0.f) || isinf(m)) return 1.f;
