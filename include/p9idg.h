@@ -58,7 +58,7 @@ enum {
  * remainder of the n table (centred on zero), and expand the last factor in powers of dw r.
  * First-order form up to P9IDG_TC_MAX_W_TERM: the term left out is at most (dw r)^2 / 2 = 5e-5 of
  * each visibility's contribution.  Second-order form (two more operand rows per visibility and a third
- * accumulator block; gridder 8 %, degridder 22 % slower) up to P9IDG_TC_MAX_W_TERM2: the term left out is at most (dw r)^3 / 6 = 4.5e-6.
+ * accumulator block; gridder 12 %, degridder 14 % slower) up to P9IDG_TC_MAX_W_TERM2: the term left out is at most (dw r)^3 / 6 = 4.5e-6.
  * Both stay inside the modes' stated 1e-4 relative-L2 bound together with their rounding.  A
  * plan picks the first-order form where it holds, else the second-order one
  * (p9idg_plan_info.tc_order); a plan beyond P9IDG_TC_MAX_W_TERM2 keeps the FP32 kernels when a

@@ -1,4 +1,5 @@
-// Tensor-core (tcgen05) gridder and degridder for S = 32, split precision.
+// Tensor-core (tcgen05) gridder and degridder, 32 operand rows per subgrid axis (S = 32, or a
+// smaller S padded to 32), split precision.
 //
 // The per-subgrid phase of the reference (Gridder.cs:61-67, 143-145) is
 //     phi_k(x, y) = du_k l_x + dv_k m_y + dw_k n(x, y)
@@ -15,20 +16,20 @@
 //              T_j = sum_x Q_j[y][x] conj(A_k(x)),  Q0 = pix, Q1 = r (.) pix   (GEMM, M = visibilities)
 // Only 2*S sincos per visibility remain (vs S^2 in the FP32 kernels); the contractions
 // run on tcgen05 with BF16 (or FP16) hi+lo operands: x ~ hi + lo, products hi*hi + hi*lo +
-// lo*hi accumulated in FP32 in tensor memory.  The P1 / T1 corrections use hi*hi only.
+// lo*hi (the gridder also forms lo*lo) accumulated in FP32 in tensor memory.  The first-order
+// rows B1 = dw B are hi only.
 //
 // Gridder MMA layout (per stage of 64 visibilities = K64, k = visibility; real and imaginary
 // parts in separate rows; both operands MN-major, so two rows of one visibility pack into one
 // BF16 pair and a lane, owning one visibility, writes 16-byte lines of 8 rows):
-//   A rows (256, y = row % 32):  [Bh_re ; Bh_im ; B1_re ; B1_im ; Bl_re ; Bl_im ; 0 ; 0]
-//       B = B_k(y) = Bh + Bl,  B1 = dw_k B_k(y) (hi only)
-//   B rows (128, x = row % 32):  [Wh_re ; Wh_im ; Wl_re ; Wl_im],  W = vis_k A_k(x) = Wh + Wl
-//   MMA1: A rows 0-127 x B rows 0-127 (M128 N128) -> TMEM cols 0..127
-//   MMA2: A rows 128-255 x B rows 0-63 (M128 N64) -> TMEM cols 0..63 (rows 64-127 of it are 0)
-//   TMEM lane quarter q = (Bh+Bl)_re, (Bh+Bl)_im, B1_re, B1_im against columns
-//   [Wh_re | Wh_im | Wl_re | Wl_im]: the lo*lo block is never formed, and
-//   P0 = sum over the W column blocks of (re.re - im.im, re.im + im.re) of lanes 0-63,
-//   P1 the same of lanes 64-127.
+//   A rows (128, x = row % 32):  [Wh_re ; Wh_im ; Wl_re ; Wl_im],  W = vis_k A_k(x) = Wh + Wl
+//   B rows (192, y = row % 32):  [Bh_re ; Bh_im ; B1_re ; B1_im ; Bl_re ; Bl_im]
+//       B = B_k(y) = Bh + Bl,  B1 = dw_k B_k(y) (hi only); second order: + [B2_re ; B2_im]
+//   one MMA per K16: M128 N192 (N256) -> TMEM lanes = the W rows, columns = the y rows
+//   A warp reads its lane quarter (one W part: hi or lo, re or im; lane = x) against the re or
+//   im y columns, and writes plane [y][x] of (Bh + Bl), of B1 (and of B2); the pixel step sums
+//   the W hi and lo planes: P0 = (re.re - im.im, re.im + im.re) of the (Bh + Bl) planes, P1 of
+//   the B1 planes.
 // Degridder (per tile of 128 visibilities = rows; k = 2x + re/im):
 //   A rows: [cos, sin](phase_A);  static B rows (192):  [B0_lo ; B0_hi ; B1_hi], each block of 64
 //       rows in groups of four (re y, re y+1, im y, im y+1), y even, so that the epilogue reads
@@ -222,15 +223,19 @@ constexpr uint32_t kGRingVis = kGVps * 16;               // visibilities after t
 constexpr uint32_t kGRingSlot = kGRingVis + kGVps * 16;  // coefficients + visibilities (complex128 at most)
 constexpr uint32_t kGSbo = kGVps / 8 * 128;              // bytes between 8-row groups of an operand
 constexpr uint32_t kGRows32 = 4 * kGSbo;                 // bytes of 32 operand rows
-constexpr uint32_t kGStageA = 256 * kGVps * 2;  // MMA1 operand (rows 0-127), then MMA2's (128-255)
-constexpr uint32_t kGStageA2 = 128 * kGVps * 2;
-constexpr uint32_t kGStageB = 128 * kGVps * 2;
-constexpr uint32_t kGStageBytes = kGStageA + kGStageB;
-constexpr uint32_t kGEpilogue = 12 * 32 * 33 * 4;  // the epilogue's 8 (12) planes reuse the stages
-static_assert(kGEpilogue <= kGStages * kGStageBytes, "epilogue planes must fit in the operand stages");
-constexpr uint32_t kGSmem = kGStages * kGStageBytes + kGRing * kGRingSlot + 512 + 1024;
-constexpr uint32_t kGTmemCols = 128;   // first order: [Wh | Wl] against the A rows of MMA1 (MMA2 adds in)
-constexpr uint32_t kGTmemCols2 = 256;  // second order: MMA2 (Bl and B2 rows) into its own columns 128-191
+constexpr uint32_t kGStageA = 128 * kGVps * 2;  // the MMA's A operand: the 128 W rows
+// its B operand: the 192 y rows (256 in the second-order form)
+__host__ __device__ constexpr uint32_t g_stage_bytes(bool o2) { return kGStageA + (o2 ? 256 : 192) * kGVps * 2; }
+// epilogue planes (32 x 33 floats each, [y][x]): 16 (24 in the second-order form), over the
+// operand stages and, in the second-order form, the input ring behind them
+constexpr uint32_t kGPlane = 32 * 33 * 4;
+static_assert(16 * kGPlane <= kGStages * g_stage_bytes(false), "first-order planes must fit in the stages");
+static_assert(24 * kGPlane <= kGStages * g_stage_bytes(true) + kGRing * kGRingSlot,
+              "second-order planes must fit in the stages and the ring");
+__host__ __device__ constexpr uint32_t g_smem(bool o2) {
+    return kGStages * g_stage_bytes(o2) + kGRing * kGRingSlot + 512 + 1024;
+}
+constexpr uint32_t kGTmemCols = 256;  // the 192 (256) columns of the y rows
 
 // The gridder epilogue's last step for the 4 pixels a producer thread finishes: P = P0 + i r P1
 // (- (r^2 / 2) P2) from the planes E, times the taper, into the work item's partial subgrid
@@ -256,29 +261,33 @@ __device__ __forceinline__ void gridder_finish(const TcArgs &a, const float *E, 
         const int p = threadIdx.x + k * kGProducerWarps * 32;
         const int y = p >> 5, x = p & 31;
         const int e = y * 33 + x;
-        const float p0re = (E[0 * 1056 + e] - E[3 * 1056 + e]) * i0;
-        const float p0im = (E[1 * 1056 + e] + E[2 * 1056 + e]) * i0;
-        const float p1re = (E[4 * 1056 + e] - E[7 * 1056 + e]) * i1;
-        const float p1im = (E[5 * 1056 + e] + E[6 * 1056 + e]) * i1;
+        // plane (kind, W part t, y part u), the W hi and lo quarters summed
+        auto pl = [&](int kind, int t, int u) {
+            return E[(kind * 8 + 2 * t + u) * 1056 + e] + E[(kind * 8 + 4 + 2 * t + u) * 1056 + e];
+        };
+        const float p0re = (pl(0, 0, 0) - pl(0, 1, 1)) * i0;
+        const float p0im = (pl(0, 0, 1) + pl(0, 1, 0)) * i0;
+        const float p1re = (pl(1, 0, 0) - pl(1, 1, 1)) * i1;
+        const float p1im = (pl(1, 0, 1) + pl(1, 1, 0)) * i1;
         const float rr = ep_r[k], tap = ep_t[k];
         float re = fmaf(-rr, p1im, p0re), im = fmaf(rr, p1re, p0im);
         if (O2) {  // - (r^2 / 2) P2
             const float h2 = rr * rr * i2;
-            re = fmaf(-h2, E[8 * 1056 + e] - E[11 * 1056 + e], re);
-            im = fmaf(-h2, E[9 * 1056 + e] + E[10 * 1056 + e], im);
+            re = fmaf(-h2, pl(2, 0, 0) - pl(2, 1, 1), re);
+            im = fmaf(-h2, pl(2, 0, 1) + pl(2, 1, 0), im);
         }
         if (y < S && x < S) out[shift_half(y, S) * S + shift_half(x, S)] = make_float2(re * tap, im * tap);
     }
 }
 
-// O2: the second-order form (|dw r| up to P9IDG_TC_MAX_W_TERM2): rows 192-255 of the A operand,
-// zero in the first-order form, carry B2 = dw^2 Bh, and MMA2 accumulates into its own columns, so
-// P = P0 + i r (.) P1 - (r^2 / 2) (.) P2 with P2 = B diag(vis dw^2) A^T.
+// O2: the second-order form (|dw r| up to P9IDG_TC_MAX_W_TERM2): y rows 192-255 carry
+// B2 = dw^2 Bh (N = 256), so P = P0 + i r (.) P1 - (r^2 / 2) (.) P2 with P2 = B diag(vis dw^2) A^T.
 template <bool BF16, typename VisT, bool BATCH, bool TMA, bool O2>
 __global__ void __launch_bounds__(kGThreads, 2)
     tc_gridder_kernel(const TcArgs L, const TcArgs *__restrict__ probs, const __grid_constant__ TmaMaps maps) {
     extern __shared__ unsigned char smem_raw[];
     unsigned char *smem = smem_1k(smem_raw);
+    constexpr uint32_t kGStageBytes = g_stage_bytes(O2);
     unsigned char *ring = smem + kGStages * kGStageBytes;
     uint64_t *full = reinterpret_cast<uint64_t *>(ring + kGRing * kGRingSlot);
     uint64_t *empty = full + kGStages;
@@ -316,19 +325,10 @@ __global__ void __launch_bounds__(kGThreads, 2)
         mbar_fence_init();
     }
     if (warp == kGMmaWarp) {
-        tmem_alloc(tmem_slot, O2 ? kGTmemCols2 : kGTmemCols);
+        tmem_alloc(tmem_slot, kGTmemCols);
         tmem_relinquish();
     }
     const uint32_t sbase = smem_u32(smem), rbase = smem_u32(ring);
-    if (!O2 && warp < kGProducerWarps) {
-        // rows 192-255 of every stage's A operand (MMA2's lower half) stay zero
-        constexpr uint32_t kZeroBytes = 64 * kGVps * 2;
-        for (uint32_t off = threadIdx.x * 16; off < kGStages * kZeroBytes; off += kGProducerWarps * 32 * 16) {
-            const uint32_t st = off / kZeroBytes, o = off % kZeroBytes;
-            st_shared_v4(sbase + st * kGStageBytes + 192 * kGVps * 2 + o, 0u, 0u, 0u, 0u);
-        }
-        fence_proxy_async();
-    }
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
@@ -337,7 +337,7 @@ __global__ void __launch_bounds__(kGThreads, 2)
     if (warp == kGMmaWarp) {
         // ---- MMA issuer ----
         if (lane == 0) {
-            constexpr uint32_t id128 = idesc_f16(128, 128, BF16, true), id64 = idesc_f16(128, 64, BF16, true);
+            constexpr uint32_t idn = idesc_f16(128, O2 ? 256 : 192, BF16, true);
             for (int i = 0; i < nstages; i++) {
                 const int s = i % kGStages;
                 const uint32_t ph = (i / kGStages) & 1;
@@ -349,15 +349,9 @@ __global__ void __launch_bounds__(kGThreads, 2)
                 tc_fence_after();
                 const uint32_t A = sbase + s * kGStageBytes, B = A + kGStageA;
 #pragma unroll
-                for (int kc = 0; kc < kGVps / 16; kc++) {
-                    const uint64_t db = smem_desc(B + kc * 256, 128, kGSbo);
-                    mma_f16(tmem, smem_desc(A + kc * 256, 128, kGSbo), db, id128, (i > 0 || kc > 0) ? 1u : 0u);
-                    if (O2)
-                        mma_f16(tmem + 128, smem_desc(A + kGStageA2 + kc * 256, 128, kGSbo), db, id64,
-                                (i > 0 || kc > 0) ? 1u : 0u);
-                    else
-                        mma_f16(tmem, smem_desc(A + kGStageA2 + kc * 256, 128, kGSbo), db, id64, 1u);
-                }
+                for (int kc = 0; kc < kGVps / 16; kc++)
+                    mma_f16(tmem, smem_desc(A + kc * 256, 128, kGSbo), smem_desc(B + kc * 256, 128, kGSbo), idn,
+                            (i > 0 || kc > 0) ? 1u : 0u);
                 mma_commit(&empty[s]);
             }
             mma_commit(accb);
@@ -539,20 +533,20 @@ __global__ void __launch_bounds__(kGThreads, 2)
             const uint32_t A = sbase + s * kGStageBytes, B = A + kGStageA;
             const uint32_t ko = static_cast<uint32_t>(rg * kGSbo + kl * 16);
 #define P9_ST(addr, r) st_shared_v4((addr), wd[0][r], wd[1][r], wd[2][r], wd[3][r])
-            P9_ST(A + ko, 0);                              // Bh_re: rows 0-31
-            P9_ST(A + kGRows32 + ko, 1);                   // Bh_im: rows 32-63
-            P9_ST(A + 2 * kGRows32 + ko, 2);               // B1_re: rows 64-95
-            P9_ST(A + 3 * kGRows32 + ko, 3);               // B1_im: rows 96-127
-            P9_ST(A + kGStageA2 + ko, 4);                  // Bl_re: rows 128-159
-            P9_ST(A + kGStageA2 + kGRows32 + ko, 5);       // Bl_im: rows 160-191
+            P9_ST(B + ko, 0);                   // Bh_re: B rows 0-31
+            P9_ST(B + kGRows32 + ko, 1);        // Bh_im: 32-63
+            P9_ST(B + 2 * kGRows32 + ko, 2);    // B1_re: 64-95
+            P9_ST(B + 3 * kGRows32 + ko, 3);    // B1_im: 96-127
+            P9_ST(B + 4 * kGRows32 + ko, 4);    // Bl_re: 128-159
+            P9_ST(B + 5 * kGRows32 + ko, 5);    // Bl_im: 160-191
             if (O2) {
-                P9_ST(A + kGStageA2 + 2 * kGRows32 + ko, O2 ? 10 : 0);  // B2_re: rows 192-223
-                P9_ST(A + kGStageA2 + 3 * kGRows32 + ko, O2 ? 11 : 0);  // B2_im: rows 224-255
+                P9_ST(B + 6 * kGRows32 + ko, O2 ? 10 : 0);  // B2_re: 192-223
+                P9_ST(B + 7 * kGRows32 + ko, O2 ? 11 : 0);  // B2_im: 224-255
             }
-            P9_ST(B + ko, 6);                              // Wh_re: rows 0-31
-            P9_ST(B + kGRows32 + ko, 7);                   // Wh_im: rows 32-63
-            P9_ST(B + 2 * kGRows32 + ko, 8);               // Wl_re: rows 64-95
-            P9_ST(B + 3 * kGRows32 + ko, 9);               // Wl_im: rows 96-127
+            P9_ST(A + ko, 6);                   // Wh_re: A rows 0-31
+            P9_ST(A + kGRows32 + ko, 7);        // Wh_im: 32-63
+            P9_ST(A + 2 * kGRows32 + ko, 8);    // Wl_re: 64-95
+            P9_ST(A + 3 * kGRows32 + ko, 9);    // Wl_im: 96-127
 #undef P9_ST
             fence_proxy_async();
             __syncwarp();
@@ -565,28 +559,33 @@ __global__ void __launch_bounds__(kGThreads, 2)
         const bool ok = warp_wait(accb, 0, abort_flag, a.wait_ns);
         tc_fence_after();
         float *E = reinterpret_cast<float *>(smem);  // the stages are free once accb completed
-        // warp: lane quarter q (rows (Bh+Bl)_re, (Bh+Bl)_im, B1_re, B1_im) against the real (h = 0)
-        // or imaginary (h = 1) columns of W, hi and lo blocks summed: plane 2q + h
-        const int q = warp & 3, h = warp >> 2;
+        // warp: TMEM lane quarter q (the W rows Wh_re, Wh_im, Wl_re, Wl_im; lane = x) against the real
+        // (u = 0) or imaginary (u = 1) y rows: plane kind * 8 + 2 q + u holds [y][x] of
+        // kind 0: (Bh + Bl) columns, 1: B1, 2: B2
+        const int q = warp & 3, u = warp >> 2;
         if (ok) {
             uint32_t r[32];
-            const uint32_t t = tmem + (static_cast<uint32_t>(32 * q) << 16) + static_cast<uint32_t>(h * 32);
-            float *e = E + (2 * q + h) * 32 * 33 + lane * 33;  // this thread's row of the plane
-            tmem_ld32(t, r);  // hi block of W
+            const uint32_t t = tmem + (static_cast<uint32_t>(32 * q) << 16) + static_cast<uint32_t>(32 * u);
+            float *e0 = E + (2 * q + u) * 1056 + lane;
+            tmem_ld32(t, r);  // Bh_u
             tmem_ld_wait(r);
 #pragma unroll
-            for (int j = 0; j < 32; j++) e[j] = __uint_as_float(r[j]);
-            tmem_ld32(t + 64, r);  // lo block of W
+            for (int j = 0; j < 32; j++) e0[j * 33] = __uint_as_float(r[j]);
+            tmem_ld32(t + 128, r);  // Bl_u
             tmem_ld_wait(r);
 #pragma unroll
-            for (int j = 0; j < 32; j++) e[j] += __uint_as_float(r[j]);
+            for (int j = 0; j < 32; j++) e0[j * 33] += __uint_as_float(r[j]);
+            float *e1 = E + (8 + 2 * q + u) * 1056 + lane;
+            tmem_ld32(t + 64, r);  // B1_u
+            tmem_ld_wait(r);
+#pragma unroll
+            for (int j = 0; j < 32; j++) e1[j * 33] = __uint_as_float(r[j]);
             if (O2) {
-                // MMA2's columns: Bl (quarters 0, 1) adds into P0's plane, B2 (quarters 2, 3) to its own
-                tmem_ld32(t + 128, r);
+                float *e2 = E + (16 + 2 * q + u) * 1056 + lane;
+                tmem_ld32(t + 192, r);  // B2_u
                 tmem_ld_wait(r);
-                float *e2 = q < 2 ? e : E + (8 + 2 * (q - 2) + h) * 32 * 33 + lane * 33;
 #pragma unroll
-                for (int j = 0; j < 32; j++) e2[j] = (q < 2 ? e2[j] : 0.f) + __uint_as_float(r[j]);
+                for (int j = 0; j < 32; j++) e2[j * 33] = __uint_as_float(r[j]);
             }
         }
         tc_fence_before();
@@ -602,7 +601,7 @@ __global__ void __launch_bounds__(kGThreads, 2)
     __syncthreads();
     if (warp == kGMmaWarp) {
         tc_fence_after();
-        tmem_dealloc(tmem, O2 ? kGTmemCols2 : kGTmemCols);
+        tmem_dealloc(tmem, kGTmemCols);
     }
 }
 
@@ -1295,9 +1294,9 @@ namespace {
 template <bool BF16, typename VisT, bool BATCH, bool TMA, bool O2>
 cudaError_t run_gridder(const TcArgs &t, const TcArgs *probs, int32_t nitems, const TmaMaps &maps,
                         cudaStream_t stream) {
-    cudaError_t e = set_smem(tc_gridder_kernel<BF16, VisT, BATCH, TMA, O2>, kGSmem);
+    cudaError_t e = set_smem(tc_gridder_kernel<BF16, VisT, BATCH, TMA, O2>, g_smem(O2));
     if (e == cudaSuccess)
-        tc_gridder_kernel<BF16, VisT, BATCH, TMA, O2><<<nitems, kGThreads, kGSmem, stream>>>(t, probs, maps);
+        tc_gridder_kernel<BF16, VisT, BATCH, TMA, O2><<<nitems, kGThreads, g_smem(O2), stream>>>(t, probs, maps);
     return e;
 }
 
