@@ -759,8 +759,8 @@ def main():
                     "work_per_launch": f"{gridded} visibilities x {S * S} pixels, one sincos + 10 flop each"}
     else:
         achieved = gridded * 10 * S * S / (kt_ms * 1e-3) / 1e12
-        # tcgen05 work actually issued per visibility: gridder 2 MMAs (M128 N128 + M128 N64, K16) per
-        # 16 visibilities; degridder 3 MMAs (N128 + N64 + N64, K16) per 128 visibilities x 4 K chunks / 128
+        # tcgen05 work actually issued per visibility: gridder one M128 N192 K16 MMA per 16 visibilities;
+        # degridder 3 MMAs (N128 + N64 + N64, K16) per 128 visibilities x 4 K chunks / 128
         phys = (2 * 128 * 192 * 16 / 16) if kern == "gridder" else (2 * 128 * 256 * 64 / 128)
         roofline = {"bound": "tensor", "achieved": achieved, "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
                     "frac": achieved / peaks["bf16_tflops"], "traffic": traffic_per_launch(kern + "_" + headline),
