@@ -183,6 +183,11 @@ struct p9idg_plan {
     std::vector<WorkItem> gitems_lyr;  // items of the other layers, then of the busiest layer
     std::vector<int32_t> sub_lyr;      // subgrid indices in the same grouping
     int32_t lyr_minor_items = 0, lyr_minor_subs = 0, lyr_major = -1;
+    // The busiest layer's part in row bands (the rows the adder writes, before the output's
+    // FFT.Shift), so that each band's rows cross the link while the next band grids: band b is
+    // items [lyr_band_items[b], lyr_band_items[b + 1]) and subgrids [lyr_band_subs[b], ...) of
+    // that part, and once it is added, rows [lyr_band_rows[b], lyr_band_rows[b + 1]) are final.
+    std::vector<int32_t> lyr_band_items, lyr_band_subs, lyr_band_rows;
     bool lyr_ready = false;
     DevBuf d_gitems_lyr, d_sub_lyr, d_zero128;
     DevBuf d_uvw_prev, d_uvw_flag;  // the previous uvw upload and the "uvw differs" flag
@@ -665,14 +670,20 @@ struct SideJoin {
     ~SideJoin() { (void)cudaStreamSynchronize(p->side); }
 };
 
-// Target w layer of each subgrid as AdderWStack.Add places it (AdderWStack.cs:38-51; -1: skipped),
-// the busiest layer by gridded time samples, and the gridder items and subgrids regrouped as
-// [every other layer | the busiest layer].  With no work outside the busiest layer there is
-// nothing to overlap and lyr_minor_items stays 0.
+// Target w layer and first destination row of each subgrid as AdderWStack.Add places it
+// (AdderWStack.cs:38-51; layer -1: skipped), the busiest layer by gridded time samples, and the
+// gridder items and subgrids regrouped as [every other layer | the busiest layer in row bands].
+// A subgrid at row y0 adds into rows y0 .. y0 + S - 1, so once the bands up to b are added, every
+// row below the first row of band b + 1 is final.  A band holds about kBandItems gridder items
+// (about four waves of the tensor-core gridder's two CTAs per SM), at most kMaxBands bands: on the
+// 3072^2 workload (13,951 items in the busiest layer) 2, 4, 8, 12, 16 and 24 bands gave GridW in
+// 8.13, 7.80, 7.56, 7.39, 7.52 and 7.82 ms, against 8.03 ms writing the layer back after all of it.
+constexpr int kBandItems = 1152, kMaxBands = 16;
+
 p9idg_status ensure_layer_split(p9idg_plan *p) {
     if (p->lyr_ready) return P9IDG_OK;
     const int N = p->c.grid_size, S = p->c.subgrid_size, W = p->c.wlayer_count;
-    std::vector<int32_t> layer(p->subs.size(), -1);
+    std::vector<int32_t> layer(p->subs.size(), -1), row(p->subs.size(), 0);
     std::vector<int64_t> work(std::max(W, 1), 0);
     for (size_t i = 0; i < p->subs.size(); i++) {
         const auto &sg = p->subs[i];
@@ -684,40 +695,73 @@ p9idg_status ensure_layer_split(p9idg_plan *p) {
         }
         if (sx >= 1 && sx < N - S && sy >= 1 && sy < N - S && sw >= 0 && sw < W) {
             layer[i] = sw;
+            row[i] = sy;
             work[sw] += sg.time_sample_count;
         }
     }
     p->lyr_major = -1;
-    int64_t best = 0, total = 0;
-    for (int k = 0; k < W; k++) {
-        total += work[k];
+    int64_t best = 0;
+    for (int k = 0; k < W; k++)
         if (work[k] > best) {
             best = work[k];
             p->lyr_major = k;
         }
-    }
     p->gitems_lyr.clear();
     p->sub_lyr.clear();
+    p->lyr_band_items.clear();
+    p->lyr_band_subs.clear();
+    p->lyr_band_rows.clear();
     p->lyr_minor_items = p->lyr_minor_subs = 0;
-    if (p->lyr_major >= 0 && total > best) {
+    if (p->lyr_major >= 0) {
         const int32_t major = p->lyr_major;
-        for (int pass = 0; pass < 2; pass++) {
-            const bool want_major = pass == 1;
-            for (const auto &it : p->gitems)
-                if ((layer[it.subgrid] == major) == want_major) p->gitems_lyr.push_back(it);
-            for (size_t i = 0; i < layer.size(); i++)
-                if ((layer[i] == major) == want_major) p->sub_lyr.push_back(static_cast<int32_t>(i));
-            if (pass == 0) {
-                p->lyr_minor_items = static_cast<int32_t>(p->gitems_lyr.size());
-                p->lyr_minor_subs = static_cast<int32_t>(p->sub_lyr.size());
-            }
+        for (const auto &it : p->gitems)
+            if (layer[it.subgrid] != major) p->gitems_lyr.push_back(it);
+        for (size_t i = 0; i < layer.size(); i++)
+            if (layer[i] != major) p->sub_lyr.push_back(static_cast<int32_t>(i));
+        p->lyr_minor_items = static_cast<int32_t>(p->gitems_lyr.size());
+        p->lyr_minor_subs = static_cast<int32_t>(p->sub_lyr.size());
+        // the busiest layer's subgrids by first row, cut into bands of about equal work
+        std::vector<int32_t> msubs;
+        for (size_t i = 0; i < layer.size(); i++)
+            if (layer[i] == major) msubs.push_back(static_cast<int32_t>(i));
+        std::stable_sort(msubs.begin(), msubs.end(), [&](int32_t a, int32_t b) { return row[a] < row[b]; });
+        int64_t mitems = 0;
+        for (const auto &it : p->gitems) mitems += layer[it.subgrid] == major;
+        const int nb = static_cast<int>(std::min<int64_t>(
+            std::min<int64_t>(kMaxBands, std::max<int64_t>(1, (mitems + kBandItems / 2) / kBandItems)),
+            static_cast<int64_t>(msubs.size())));
+        std::vector<int32_t> band(p->subs.size(), -1);
+        int64_t acc = 0;
+        int b = 0;
+        for (int32_t i : msubs) {
+            band[i] = b;
+            acc += p->subs[i].time_sample_count;
+            if (b + 1 < nb && acc * nb >= best * (b + 1)) b++;
         }
-        CK(p->d_gitems_lyr.ensure(sizeof(WorkItem) * p->gitems_lyr.size()));
-        CK(p->d_sub_lyr.ensure(sizeof(int32_t) * p->sub_lyr.size()));
-        CK(cudaMemcpyAsync(p->d_gitems_lyr.p, p->gitems_lyr.data(), sizeof(WorkItem) * p->gitems_lyr.size(),
-                           cudaMemcpyHostToDevice, p->stream));
-        CK(cudaMemcpyAsync(p->d_sub_lyr.p, p->sub_lyr.data(), sizeof(int32_t) * p->sub_lyr.size(),
-                           cudaMemcpyHostToDevice, p->stream));
+        p->lyr_band_rows.assign(nb + 1, N);
+        p->lyr_band_rows[0] = 0;
+        for (int32_t i : msubs)  // first row of each band (the bands are in row order)
+            if (band[i] > 0) p->lyr_band_rows[band[i]] = std::min(p->lyr_band_rows[band[i]], row[i]);
+        for (int k = nb - 1; k >= 1; k--)  // a band that received no subgrid ends where the next starts
+            p->lyr_band_rows[k] = std::min(p->lyr_band_rows[k], p->lyr_band_rows[k + 1]);
+        p->lyr_band_items.push_back(0);
+        p->lyr_band_subs.push_back(0);
+        for (int k = 0; k < nb; k++) {
+            for (const auto &it : p->gitems)  // largest first within the band, as gitems is
+                if (layer[it.subgrid] == major && band[it.subgrid] == k) p->gitems_lyr.push_back(it);
+            for (int32_t i : msubs)
+                if (band[i] == k) p->sub_lyr.push_back(i);
+            p->lyr_band_items.push_back(static_cast<int32_t>(p->gitems_lyr.size()) - p->lyr_minor_items);
+            p->lyr_band_subs.push_back(static_cast<int32_t>(p->sub_lyr.size()) - p->lyr_minor_subs);
+        }
+        CK(p->d_gitems_lyr.ensure(sizeof(WorkItem) * std::max<size_t>(1, p->gitems_lyr.size())));
+        CK(p->d_sub_lyr.ensure(sizeof(int32_t) * std::max<size_t>(1, p->sub_lyr.size())));
+        if (!p->gitems_lyr.empty())
+            CK(cudaMemcpyAsync(p->d_gitems_lyr.p, p->gitems_lyr.data(), sizeof(WorkItem) * p->gitems_lyr.size(),
+                               cudaMemcpyHostToDevice, p->stream));
+        if (!p->sub_lyr.empty())
+            CK(cudaMemcpyAsync(p->d_sub_lyr.p, p->sub_lyr.data(), sizeof(int32_t) * p->sub_lyr.size(),
+                               cudaMemcpyHostToDevice, p->stream));
         CK(cudaStreamSynchronize(p->stream));
     }
     p->lyr_ready = true;
@@ -752,6 +796,24 @@ p9idg_status layer_to_host(const float2 *d_layer, size_t nn, double2 *h_out, dou
     return P9IDG_OK;
 }
 
+// Rows [r0, r1) of one complex64 layer, as the adder numbers them (before the FFT.Shift the layer
+// is stored with), -> the same rows of the caller's complex128 layer: the shifted rows of the range
+// form at most two contiguous runs (three for an odd N), each widened and copied on its own.
+p9idg_status layer_rows_to_host(const float2 *d_layer, int N, int r0, int r1, double2 *h_out, double2 *d_stage,
+                                bool pinned, cudaStream_t st) {
+    const int n2 = N / 2, m = 2 * n2;
+    auto stored = [&](int r) { return r < m ? (r + n2 < m ? r + n2 : r - n2) : r; };  // shift_index's row map
+    for (int r = r0; r < r1;) {
+        const int a = stored(r);
+        int len = 1;
+        while (r + len < r1 && stored(r + len) == a + len) len++;
+        const size_t off = static_cast<size_t>(a) * N, count = static_cast<size_t>(len) * N;
+        TRY(layer_to_host(d_layer + off, count, h_out + off, pinned ? d_stage + off : nullptr, pinned, st));
+        r += len;
+    }
+    return P9IDG_OK;
+}
+
 // Zeros one complex128 layer of the caller's output in host memory.
 p9idg_status zero_host_layer(p9idg_plan *p, double2 *h_out, size_t nn, bool pinned, cudaStream_t st) {
     if (pinned) {
@@ -781,12 +843,12 @@ p9idg_status host_grid_common(p9idg_plan *p, const double *vis, const double *uv
         const size_t nn = nn_of(p);
         CK(p->d_layers.ensure(sizeof(float2) * nl * nn));
         std::vector<char> used(nl, 1);
-        bool split = false;
+        bool banded = false;
         if (wstack) {
             TRY(ensure_gaps(p));
             used.assign(p->layer_used.begin(), p->layer_used.begin() + nl);
             TRY(ensure_layer_split(p));
-            split = p->lyr_minor_items > 0;
+            banded = p->lyr_major >= 0 && !p->lyr_band_rows.empty();
         }
         auto *out128 = reinterpret_cast<double2 *>(out);
         const bool pinned = host_pinned(out, sizeof(double2) * nl * nn);
@@ -803,7 +865,7 @@ p9idg_status host_grid_common(p9idg_plan *p, const double *vis, const double *uv
             if (!used[k]) TRY(zero_host_layer(p, out128 + k * nn, nn, pinned, p->side));
         TRY(upload_uvw(p, uvw));  // host-to-device, beside the zero-fill
         float2 *layers = p->d_layers.as<float2>();
-        if (!split) {
+        if (!banded) {
             TRY(run_grid(p, vis, true, layers, wstack));
             StageScope t(p, P9IDG_STAGE_D2H);
             for (size_t k = 0; k < nl; k++)
@@ -815,19 +877,30 @@ p9idg_status host_grid_common(p9idg_plan *p, const double *vis, const double *uv
             const int32_t *subl = p->d_sub_lyr.as<int32_t>();
             const int32_t nmi = p->lyr_minor_items, nms = p->lyr_minor_subs;
             const size_t major = static_cast<size_t>(p->lyr_major);
-            TRY(grid_items(p, vis, true, items, nmi));
-            TRY(add_subgrids(p, layers, true, subl, nms, static_cast<int>(nl)));
-            CK(cudaEventRecord(p->ev_mid, p->stream));
-            CK(cudaStreamWaitEvent(p->side, p->ev_mid, 0));
-            for (size_t k = 0; k < nl; k++)
-                if (used[k] && k != major)
-                    TRY(layer_to_host(layers + k * nn, nn, out128 + k * nn, stage(k), pinned,
-                                      p->side));
-            TRY(grid_items(p, vis, true, items + nmi, static_cast<int32_t>(p->gitems_lyr.size()) - nmi));
-            TRY(add_subgrids(p, layers, true, subl + nms, static_cast<int32_t>(p->sub_lyr.size()) - nms, 0));
-            StageScope t(p, P9IDG_STAGE_D2H);
-            TRY(layer_to_host(layers + major * nn, nn, out128 + major * nn, stage(major), pinned,
-                              p->stream));
+            int clear = static_cast<int>(nl);  // the first add zeroes every layer
+            if (nmi > 0 || nms > 0) {
+                TRY(grid_items(p, vis, true, items, nmi));
+                TRY(add_subgrids(p, layers, true, subl, nms, clear));
+                clear = 0;
+                CK(cudaEventRecord(p->ev_mid, p->stream));
+                CK(cudaStreamWaitEvent(p->side, p->ev_mid, 0));
+                for (size_t k = 0; k < nl; k++)
+                    if (used[k] && k != major)
+                        TRY(layer_to_host(layers + k * nn, nn, out128 + k * nn, stage(k), pinned,
+                                          p->side));
+            }
+            const auto &bi = p->lyr_band_items, &bs = p->lyr_band_subs, &br = p->lyr_band_rows;
+            const int N = p->c.grid_size;
+            for (size_t b = 0; b + 1 < br.size(); b++) {
+                TRY(grid_items(p, vis, true, items + nmi + bi[b], bi[b + 1] - bi[b]));
+                TRY(add_subgrids(p, layers, true, subl + nms + bs[b], bs[b + 1] - bs[b], clear));
+                clear = 0;
+                // the band's final rows cross the link while the next band grids
+                CK(cudaEventRecord(p->ev_mid, p->stream));
+                CK(cudaStreamWaitEvent(p->side, p->ev_mid, 0));
+                TRY(layer_rows_to_host(layers + major * nn, N, br[b], br[b + 1], out128 + major * nn,
+                                       stage(major), pinned, p->side));
+            }
         }
         CK(cudaEventRecord(p->ev_join, p->side));
         CK(cudaStreamWaitEvent(p->stream, p->ev_join, 0));

@@ -205,9 +205,10 @@ def test_empty_plan_and_stage_timing(need_gpu):
     part.plan.enable_timing(True)
     pkg.IDG.GridW(c, part, obs.vis, obs.uvw, obs.frequencies)
     t = part.plan.stage_times()
-    # one gridder + adder pass, or one per layer group when host arrays are used in place
+    # one gridder + adder pass; with host arrays used in place, one for the other w layers and one
+    # per row band (up to 4) of the busiest layer
     n = t["gridder"][1]
-    assert n in (1, 2) and t["gridder"][0] > 0 and t["subgrid_ifft_add"][1] == n
+    assert 1 <= n <= 5 and t["gridder"][0] > 0 and t["subgrid_ifft_add"][1] == n
 
 
 def test_sincos_probe(need_gpu):
