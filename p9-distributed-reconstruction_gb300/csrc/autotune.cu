@@ -85,7 +85,7 @@ extern "C" p9idg_status p9idg_autotune(const p9idg_params *c, const double *uvw,
     }
     const bool fp32 = mode == P9IDG_MODE_FP32;
     const std::vector<int> gchunks = fp32 ? std::vector<int>{512, 1024, 2048} : std::vector<int>{2048, 4096, 8192};
-    const std::vector<int> dchunks = fp32 ? std::vector<int>{256, 512, 1024} : std::vector<int>{4096, 8192, 16384};
+    const std::vector<int> dchunks = fp32 ? std::vector<int>{256, 512, 1024} : std::vector<int>{8192, 16384, 32768};
     std::vector<Candidate> results;
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);

@@ -24,7 +24,7 @@ struct TcPlanState {
     void *ditems = nullptr;       // degridder work items (<= degrid_chunk visibilities)
     int32_t nditems = 0;
     std::vector<WorkItem> ditems_host;  // the same list on the host (batches merge them)
-    int64_t degrid_chunk = 8192;        // visibilities per degridder work item (set before tc_prepare)
+    int64_t degrid_chunk = 16384;       // visibilities per degridder work item (set before tc_prepare)
     double max_w_r = 0;           // max |dw| * max |r|: bound on the phase the form expands
     double r_max = 0;             // max |r| of the centred remainder table
     int want_order = 0;           // 0: the lowest order whose bound holds; 2: always the second-order form
