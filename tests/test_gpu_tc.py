@@ -127,6 +127,35 @@ def test_tc_edge_shapes(need_gpu, mode, nch, nt, N, chunks):
     assert rel_l2(vis, ref) < TOL_TC
 
 
+SMALL_S_EDGE_SHAPES = [
+    (16, 4, 1, 37, 255, None),        # odd grid size, one channel
+    (24, 8, 3, 301, 256, (384, 384)),    # several partial subgrids per subgrid
+    (8, 2, 5, 120, 129, None),        # odd grid size, subgrids of 8 pixels
+]
+
+
+@pytest.mark.parametrize("mode", MODES)
+@pytest.mark.parametrize("S,kernel,nch,nt,N,chunks", SMALL_S_EDGE_SHAPES)
+def test_tc_smaller_subgrid_edge_shapes(need_gpu, mode, S, kernel, nch, nt, N, chunks):
+    """The padded small-subgrid path on the edge shapes: odd grid sizes (the FFT.Shift keeps the
+    last row and column), one channel, and work items split across a subgrid."""
+    obs, cd = workload("small_256", n_ant=9, nt=nt, nch=nch, seed=nch * 100 + nt + S)
+    c, cd = constants(cd, grid_size=N, subgrid_size=S, kernel_size=kernel)
+    part = pkg.Partitioner.CreatePartition(c, obs.uvw, obs.frequencies)
+    assert part.plan.set_mode(mode) == mode
+    if chunks:
+        pkg.set_chunking(part.plan, *chunks)
+    subs = oracle.partition(cd, obs.uvw, obs.frequencies)
+    assert len(subs) > 0
+    got = pkg.IDG.GridW(c, part, obs.vis, obs.uvw, obs.frequencies)
+    assert rel_l2(got, oracle.idg_grid_w(cd, subs, obs.vis, obs.uvw, obs.frequencies)) < TOL_TC
+    rng = np.random.default_rng(N + S)
+    model = rng.standard_normal((N, N)) + 1j * rng.standard_normal((N, N))
+    vis = pkg.IDG.DeGridW(c, part, model.copy(), obs.uvw, obs.frequencies)
+    ref, _ = oracle.idg_degrid(cd, subs, model, obs.uvw, obs.frequencies, wstack=True)
+    assert rel_l2(vis, ref) < TOL_TC
+
+
 @pytest.mark.parametrize("mode", MODES)
 @pytest.mark.parametrize("nch,nt,N,chunks", EDGE_SHAPES)
 def test_tc_edge_shapes_device(need_gpu, mode, nch, nt, N, chunks):
