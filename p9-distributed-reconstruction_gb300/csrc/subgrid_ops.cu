@@ -27,8 +27,10 @@ constexpr int kThreads = 256;
 // One pass of the 2-D transform over S lines (ROWS: dst[y][k] = sum_x src[y][x] w^(x k); else
 // dst[k][x] = sum_y src[y][x] w^(y k)), times scale, with w = tw[1] = exp(sign 2 pi i / S).
 // Radix-4 split: with Q = S / 4 the outputs k + Q j (j < 4) of a line come from the four sums
-// P_m(k) = sum over x = m (mod 4) of a_x w^(x k) through a 4-point DFT with root w^Q = sign i,
-// so each thread makes four outputs from S complex multiply-adds.
+// P_r(k) = sum over x = 4 m + r of a_x w^(x k) = w^(r k) sum_m a_(4m+r) w^(4 m k) through a
+// 4-point DFT with root w^Q = sign i.  A thread keeps its Q twiddles w^(4 m k) in registers and
+// applies w^(r k) once per sum, so a pass reads S inputs and Q + 3 twiddles from shared memory
+// per four outputs (the pass is bound by the shared-memory pipe) for S complex multiply-adds.
 template <int S, bool ROWS>
 __device__ __forceinline__ void dft_pass(float2 (*src)[S + 1], float2 (*dst)[S + 1], const float2 *tw, float sign,
                                          float scale) {
@@ -36,15 +38,33 @@ __device__ __forceinline__ void dft_pass(float2 (*src)[S + 1], float2 (*dst)[S +
     constexpr int Q = S / 4;
     for (int t = threadIdx.x; t < S * Q; t += kThreads) {
         const int line = t / Q, k = t - (t / Q) * Q;
-        float2 P[4] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
-        int e = 0;
+        float2 v[Q];  // w^(4 m k)
+        {
+            int e = 0, step = (4 * k) % S;
 #pragma unroll
-        for (int x = 0; x < S; x++) {
-            const float2 a = ROWS ? src[line][x] : src[x][line], w = tw[e];
-            P[x & 3].x = fmaf(a.x, w.x, fmaf(-a.y, w.y, P[x & 3].x));
-            P[x & 3].y = fmaf(a.x, w.y, fmaf(a.y, w.x, P[x & 3].y));
-            e += k;
-            if (e >= S) e -= S;
+            for (int m = 0; m < Q; m++) {
+                v[m] = tw[e];
+                e += step;
+                if (e >= S) e -= S;
+            }
+        }
+        float2 R[4] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+#pragma unroll
+        for (int m = 0; m < Q; m++) {
+#pragma unroll
+            for (int r = 0; r < 4; r++) {
+                const int x = 4 * m + r;
+                const float2 a = ROWS ? src[line][x] : src[x][line], w = v[m];
+                R[r].x = fmaf(a.x, w.x, fmaf(-a.y, w.y, R[r].x));
+                R[r].y = fmaf(a.x, w.y, fmaf(a.y, w.x, R[r].y));
+            }
+        }
+        float2 P[4];
+        P[0] = R[0];
+#pragma unroll
+        for (int r = 1; r < 4; r++) {  // times w^(r k)
+            const float2 w = tw[(r * k) % S];
+            P[r] = make_float2(fmaf(R[r].x, w.x, -R[r].y * w.y), fmaf(R[r].x, w.y, R[r].y * w.x));
         }
         const float2 A = make_float2(P[0].x + P[2].x, P[0].y + P[2].y), B = make_float2(P[0].x - P[2].x, P[0].y - P[2].y);
         const float2 C = make_float2(P[1].x + P[3].x, P[1].y + P[3].y);
@@ -99,8 +119,11 @@ __device__ __forceinline__ const SubgridOpArgs &block_args(const SubgridOpArgs &
     return L;
 }
 
+// 8 CTAs per SM (32 registers) up to S = 32: 0.173 against 0.182 ms at 3072^2 with the 40
+// registers the compiler picks unbounded (its partial-subgrid loads need the resident CTAs more
+// than registers); S = 48 fits 6 CTAs by shared memory (40 registers)
 template <int S, bool WSTACK, bool BATCH>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, S <= 32 ? 8 : 6)
     subgrid_ifft_add_kernel(const SubgridOpArgs L, const SubgridOpArgs *__restrict__ probs) {
     __shared__ float2 buf[S][S + 1];
     __shared__ float2 tmp[S][S + 1];
