@@ -6,7 +6,7 @@ and images; exact known answers to 1e-5; adjoint identities to FP32 rounding (1e
 import numpy as np
 import pytest
 
-from conftest import C_LIGHT, constants, kat_constants, oracle, pkg, rel_l2, synth, workload
+from conftest import C_LIGHT, constants, kat_constants, oracle, pkg, rel_l2, workload
 
 pytestmark = pytest.mark.gpu
 TOL = 1e-5
