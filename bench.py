@@ -797,8 +797,11 @@ def main():
         plan.set_stream(0)
         pkg.IDG.GridW(c, part, h_vis, h_uvw, obs.frequencies, out=h_layers)  # warm-up of the host path
         pkg.IDG.DeGridW(c, part, h_grid, h_uvw, obs.frequencies, out=h_vout)
-        steps_e2e = max(1, min(args.steps, 5))
+        # ten steps: a transient stall of the host's page-locked copies (seen on this pool for tens of
+        # milliseconds at a time) weighs half what it would over five; the per-step spread is reported
+        steps_e2e = max(1, min(args.steps, 10))
         t_grid = t_degrid = 0.0
+        step_ms = []
         plan.reset_timing()
         plan.enable_timing(True)  # CUDA events on the plan's stream between stages (boundary copies)
         t0 = time.perf_counter()
@@ -807,8 +810,10 @@ def main():
             pkg.IDG.GridW(c, part, h_vis, h_uvw, obs.frequencies, out=h_layers)
             tb = time.perf_counter()
             pkg.IDG.DeGridW(c, part, h_grid, h_uvw, obs.frequencies, out=h_vout)
+            tc = time.perf_counter()
             t_grid += tb - ta
-            t_degrid += time.perf_counter() - tb
+            t_degrid += tc - tb
+            step_ms.append(1e3 * (tc - ta))
         t_e2e = time.perf_counter() - t0
         if ws > 1:  # the job's time is the slowest rank's (no host-side grid reduce in this form)
             tt = torch.tensor([t_e2e], dtype=torch.float64, device="cuda")
@@ -839,6 +844,8 @@ def main():
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                "host_arrays_in_place": in_place,
                "grid_w_ms": 1e3 * t_grid / steps_e2e, "degrid_w_ms": 1e3 * t_degrid / steps_e2e,
+               "step_ms": {"min": min(step_ms), "median": float(np.median(step_ms)), "max": max(step_ms),
+                           "steps": steps_e2e},
                "stage_ms_per_step": {k: round(v[0] / steps_e2e, 4) for k, v in e2e_stages.items() if v[1]},
                "uvw_kept_on_device": {"value": 2 * total_gridded * steps_e2e / t_res / 1e6, "unit": "Mvis/s",
                                       "ms_per_step": 1e3 * t_res / steps_e2e,

@@ -13,8 +13,9 @@
 //    into the read index.
 //
 // One CTA per subgrid.  The S x S transform is two passes of S-point DFTs against a
-// twiddle table in shared memory, each split radix-4 (S is 8..48: a quarter of the O(S^3)
-// multiply-adds, against the gridder's O(vis * S^2) work).
+// twiddle table in shared memory, each split radix-4 and then in two (S is 8..48, all
+// multiples of 8: an eighth of the O(S^3) multiply-adds, against the gridder's O(vis * S^2)
+// work).
 
 #include "kernels.cuh"
 
@@ -29,15 +30,17 @@ constexpr int kThreads = 256;
 // Radix-4 split: with Q = S / 4 the outputs k + Q j (j < 4) of a line come from the four sums
 // P_r(k) = sum over x = 4 m + r of a_x w^(x k) = w^(r k) sum_m a_(4m+r) w^(4 m k) through a
 // 4-point DFT with root w^Q = sign i.  A thread keeps its Q twiddles w^(4 m k) in registers and
-// applies w^(r k) once per sum, so a pass reads S inputs and Q + 3 twiddles from shared memory
-// per four outputs (the pass is bound by the shared-memory pipe) for S complex multiply-adds.
+// applies w^(r k) once per sum; and as w^(4 m (k + Q/2)) = (-1)^m w^(4 m k), the even-m and
+// odd-m halves of its sums give the outputs of k and of k + Q/2 together.  A pass thus reads S
+// inputs and Q + 6 twiddles from shared memory per eight outputs (the pass is bound by the
+// shared-memory pipe) for S complex multiply-adds.
 template <int S, bool ROWS>
 __device__ __forceinline__ void dft_pass(float2 (*src)[S + 1], float2 (*dst)[S + 1], const float2 *tw, float sign,
                                          float scale) {
-    static_assert(S % 4 == 0, "radix-4 split needs S divisible by 4");
-    constexpr int Q = S / 4;
-    for (int t = threadIdx.x; t < S * Q; t += kThreads) {
-        const int line = t / Q, k = t - (t / Q) * Q;
+    static_assert(S % 8 == 0, "the split needs S divisible by 8");
+    constexpr int Q = S / 4, H = Q / 2;
+    for (int t = threadIdx.x; t < S * H; t += kThreads) {
+        const int line = t / H, k = t - (t / H) * H;
         float2 v[Q];  // w^(4 m k)
         {
             int e = 0, step = (4 * k) % S;
@@ -48,36 +51,47 @@ __device__ __forceinline__ void dft_pass(float2 (*src)[S + 1], float2 (*dst)[S +
                 if (e >= S) e -= S;
             }
         }
-        float2 R[4] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+        float2 Ev[4], Od[4];
+#pragma unroll
+        for (int r = 0; r < 4; r++) Ev[r] = Od[r] = make_float2(0.f, 0.f);
 #pragma unroll
         for (int m = 0; m < Q; m++) {
 #pragma unroll
             for (int r = 0; r < 4; r++) {
                 const int x = 4 * m + r;
                 const float2 a = ROWS ? src[line][x] : src[x][line], w = v[m];
-                R[r].x = fmaf(a.x, w.x, fmaf(-a.y, w.y, R[r].x));
-                R[r].y = fmaf(a.x, w.y, fmaf(a.y, w.x, R[r].y));
+                float2 &acc = (m & 1) ? Od[r] : Ev[r];
+                acc.x = fmaf(a.x, w.x, fmaf(-a.y, w.y, acc.x));
+                acc.y = fmaf(a.x, w.y, fmaf(a.y, w.x, acc.y));
             }
         }
-        float2 P[4];
-        P[0] = R[0];
 #pragma unroll
-        for (int r = 1; r < 4; r++) {  // times w^(r k)
-            const float2 w = tw[(r * k) % S];
-            P[r] = make_float2(fmaf(R[r].x, w.x, -R[r].y * w.y), fmaf(R[r].x, w.y, R[r].y * w.x));
-        }
-        const float2 A = make_float2(P[0].x + P[2].x, P[0].y + P[2].y), B = make_float2(P[0].x - P[2].x, P[0].y - P[2].y);
-        const float2 C = make_float2(P[1].x + P[3].x, P[1].y + P[3].y);
-        const float2 D = make_float2(-sign * (P[1].y - P[3].y), sign * (P[1].x - P[3].x));  // sign i (P1 - P3)
-        const float2 X[4] = {make_float2(A.x + C.x, A.y + C.y), make_float2(B.x + D.x, B.y + D.y),
-                             make_float2(A.x - C.x, A.y - C.y), make_float2(B.x - D.x, B.y - D.y)};
+        for (int half = 0; half < 2; half++) {
+            const int kk = k + half * H;
+            float2 P[4];
 #pragma unroll
-        for (int j = 0; j < 4; j++) {
-            const float2 v = make_float2(X[j].x * scale, X[j].y * scale);
-            if (ROWS)
-                dst[line][k + Q * j] = v;
-            else
-                dst[k + Q * j][line] = v;
+            for (int r = 0; r < 4; r++)
+                P[r] = half ? make_float2(Ev[r].x - Od[r].x, Ev[r].y - Od[r].y)
+                            : make_float2(Ev[r].x + Od[r].x, Ev[r].y + Od[r].y);
+#pragma unroll
+            for (int r = 1; r < 4; r++) {  // times w^(r kk)
+                const float2 w = tw[(r * kk) % S];
+                P[r] = make_float2(fmaf(P[r].x, w.x, -P[r].y * w.y), fmaf(P[r].x, w.y, P[r].y * w.x));
+            }
+            const float2 A = make_float2(P[0].x + P[2].x, P[0].y + P[2].y),
+                         B = make_float2(P[0].x - P[2].x, P[0].y - P[2].y);
+            const float2 C = make_float2(P[1].x + P[3].x, P[1].y + P[3].y);
+            const float2 D = make_float2(-sign * (P[1].y - P[3].y), sign * (P[1].x - P[3].x));  // sign i (P1 - P3)
+            const float2 X[4] = {make_float2(A.x + C.x, A.y + C.y), make_float2(B.x + D.x, B.y + D.y),
+                                 make_float2(A.x - C.x, A.y - C.y), make_float2(B.x - D.x, B.y - D.y)};
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const float2 val = make_float2(X[j].x * scale, X[j].y * scale);
+                if (ROWS)
+                    dst[line][kk + Q * j] = val;
+                else
+                    dst[kk + Q * j][line] = val;
+            }
         }
     }
     __syncthreads();
@@ -119,9 +133,9 @@ __device__ __forceinline__ const SubgridOpArgs &block_args(const SubgridOpArgs &
     return L;
 }
 
-// 8 CTAs per SM (32 registers) up to S = 32: 0.173 against 0.182 ms at 3072^2 with the 40
-// registers the compiler picks unbounded (its partial-subgrid loads need the resident CTAs more
-// than registers); S = 48 fits 6 CTAs by shared memory (40 registers)
+// 8 CTAs per SM (32 registers) up to S = 32: 0.164 ms at 3072^2 against 0.170 ms at 6 CTAs per
+// SM (its partial-subgrid loads need the resident CTAs more than registers); S = 48 fits 6 CTAs
+// by shared memory (40 registers)
 template <int S, bool WSTACK, bool BATCH>
 __global__ void __launch_bounds__(kThreads, S <= 32 ? 8 : 6)
     subgrid_ifft_add_kernel(const SubgridOpArgs L, const SubgridOpArgs *__restrict__ probs) {
