@@ -265,7 +265,9 @@ void p9idg_batch_destroy(p9idg_batch *batch);
 
 /* Autotuner: times grid + degrid on a sample of the observation's baselines for each candidate
  * subgrid size (and work-item size) and returns the fastest per gridded visibility among the
- * candidates that drop no more visibilities than the best of them. */
+ * candidates that grid at least 99.9 % of the best candidate's gridded visibilities.
+ * subgrid_sizes NULL (or nsizes 0): 24, 32 and 48; a size the mode does not run (48 in a
+ * tensor-core mode) or a plan it rules out is skipped. */
 typedef struct p9idg_tuning {
     int32_t subgrid_size;
     int32_t kernel_size;
