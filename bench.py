@@ -715,7 +715,9 @@ def main():
                              value=2 * total_gridded * args.steps / (ms * 1e-3) / 1e6)
     head = results[headline]
     stages = head["stages"]
-    launches = sum(n for (_, n) in stages.values()) - stages["h2d"][1] - stages["d2h"][1]
+    # one launch per timed stage, plus the two zero-fills each step runs beside the gridder (w layers)
+    # and the degridder (uncovered visibilities), outside the stages
+    launches = sum(n for (_, n) in stages.values()) - stages["h2d"][1] - stages["d2h"][1] + 2 * args.steps
 
     # tensor-core vs FP32 kernels on the whole workload: w layers, degridded visibilities, dirty image
     tc_vs_fp32 = None

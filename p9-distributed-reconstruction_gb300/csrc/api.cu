@@ -177,6 +177,10 @@ struct p9idg_plan {
     DevBuf d_gaps;
     cudaStream_t side = nullptr;  // the D2H copy of DeGrid's shifted grid runs here, beside the degridder
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_mid = nullptr;
+    // Zero-fills beside the gridder and degridder (ZeroSide): a high-priority stream, so that its few
+    // CTAs take the room the kernels leave on each SM instead of queueing behind their work items.
+    cudaStream_t zside = nullptr;
+    cudaEvent_t ev_zfork = nullptr, ev_zjoin = nullptr;
     // In-place GridW: the gridder items and the subgrids regrouped so that every w layer but the
     // busiest one is gridded and added first; those layers then cross the link while the busiest
     // one grids.  Items keep their partial-subgrid slots; built with the gridder items.
@@ -332,6 +336,13 @@ p9idg_status ensure_device(p9idg_plan *p) {
     if (!p->ev_fork) CK(cudaEventCreateWithFlags(&p->ev_fork, cudaEventDisableTiming));
     if (!p->ev_join) CK(cudaEventCreateWithFlags(&p->ev_join, cudaEventDisableTiming));
     if (!p->ev_mid) CK(cudaEventCreateWithFlags(&p->ev_mid, cudaEventDisableTiming));
+    if (!p->zside) {
+        int least = 0, greatest = 0;
+        CK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        CK(cudaStreamCreateWithPriority(&p->zside, cudaStreamNonBlocking, greatest));
+    }
+    if (!p->ev_zfork) CK(cudaEventCreateWithFlags(&p->ev_zfork, cudaEventDisableTiming));
+    if (!p->ev_zjoin) CK(cudaEventCreateWithFlags(&p->ev_zjoin, cudaEventDisableTiming));
     {
         int pageable = 0, host_tables = 0;
         CK(cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, p->device));
@@ -502,6 +513,32 @@ p9idg_status check_wstack_layers(const p9idg_plan *p) {
 size_t vis_count_of(const p9idg_plan *p) { return static_cast<size_t>(p->nbl) * p->nt * p->nch; }
 size_t nn_of(const p9idg_plan *p) { return static_cast<size_t>(p->c.grid_size) * p->c.grid_size; }
 
+// A zero-fill of output memory that the kernels queued meanwhile on the plan's stream do not touch
+// (the w layers while the gridder writes its partial subgrids; the visibilities no subgrid covers
+// while the splitter and degridder write the others), run on the zeroing stream: fork() before those
+// kernels, the fill launched after them (so that their first CTAs are placed first), join() before
+// the first kernel that needs it.  A call that returns early with an error waits for the fill on
+// the host, so none outlives the call.
+struct ZeroSide {
+    p9idg_plan *p;
+    bool forked = false, joined = false;
+    p9idg_status fork() {
+        CK(cudaEventRecord(p->ev_zfork, p->stream));
+        CK(cudaStreamWaitEvent(p->zside, p->ev_zfork, 0));
+        forked = true;
+        return P9IDG_OK;
+    }
+    p9idg_status join() {
+        CK(cudaEventRecord(p->ev_zjoin, p->zside));
+        CK(cudaStreamWaitEvent(p->stream, p->ev_zjoin, 0));
+        joined = true;
+        return P9IDG_OK;
+    }
+    ~ZeroSide() {
+        if (forked && !joined) (void)cudaStreamSynchronize(p->zside);
+    }
+};
+
 // Gridder over nitems work items (all of the plan's, or a group of them) into their partial slots.
 p9idg_status grid_items(p9idg_plan *p, const void *d_vis, bool vis_c128, const WorkItem *d_items, int32_t nitems) {
     const int S = p->c.subgrid_size;
@@ -522,13 +559,9 @@ p9idg_status grid_items(p9idg_plan *p, const void *d_vis, bool vis_c128, const W
     return P9IDG_OK;
 }
 
-// Subgrid IFFT + adder of nsub subgrids (all, or the subgrid list d_list) into the layers,
-// after zeroing the first clear_nl layers (one timed stage either way).
-p9idg_status add_subgrids(p9idg_plan *p, float2 *d_layers, bool wstack, const int32_t *d_list, int32_t nsub,
-                          int clear_nl) {
+// Subgrid IFFT + adder of nsub subgrids (all, or the subgrid list d_list) into the layers.
+p9idg_status add_subgrids(p9idg_plan *p, float2 *d_layers, bool wstack, const int32_t *d_list, int32_t nsub) {
     StageScope t(p, P9IDG_STAGE_SUBGRID_IFFT_ADD);
-    if (clear_nl > 0)
-        CK(cudaMemsetAsync(d_layers, 0, sizeof(float2) * static_cast<size_t>(clear_nl) * nn_of(p), p->stream));
     SubgridOpArgs a = subgrid_args(p);
     a.partials = p->d_partials.as<float2>();
     a.layers = d_layers;
@@ -542,21 +575,34 @@ p9idg_status add_subgrids(p9idg_plan *p, float2 *d_layers, bool wstack, const in
     return P9IDG_OK;
 }
 
+// The layers are zeroed beside the gridder (a 604 MB fill at 3072^2 with 8 layers, 0.09 ms of the
+// adder's stage when it ran there).
 p9idg_status run_grid(p9idg_plan *p, const void *d_vis, bool vis_c128, float2 *d_layers, bool wstack) {
     const int nl = wstack ? p->c.wlayer_count : 1;
+    ZeroSide z{p};
+    TRY(z.fork());
     TRY(grid_items(p, d_vis, vis_c128, p->d_gitems.as<WorkItem>(), static_cast<int32_t>(p->gitems.size())));
-    return add_subgrids(p, d_layers, wstack, nullptr, 0, nl);
+    CK(launch_zero_c64_beside(d_layers, static_cast<int64_t>(nl) * static_cast<int64_t>(nn_of(p)), p->zside));
+    TRY(z.join());
+    return add_subgrids(p, d_layers, wstack, nullptr, 0);
 }
 
 // grid (device complex64) -> vis (device, complex64 or complex128); uncovered samples are 0
 p9idg_status ensure_gaps(p9idg_plan *p);
 
-// zero_gaps: zero only the visibilities no subgrid covers (the degridder writes every other one)
-// instead of the whole output -- for an output in host memory, where every byte crosses the link.
+// The degridder writes every visibility some subgrid covers; only the others (quirk P1's drops,
+// baselines without subgrids) are zeroed apart.  Output in host memory (out_in_host): before the
+// degridder, on the plan's stream.  Output in device memory: beside the splitter and degridder, on
+// the zeroing stream, as the two write disjoint visibilities (the whole output, 516 MB at 3072^2,
+// was zeroed before the degridder, 0.08 ms of its stage).
 p9idg_status run_degrid(p9idg_plan *p, const float2 *d_grid, bool grid_shifted, void *d_vis, bool out_c128,
-                        bool wstack, bool zero_gaps = false) {
+                        bool wstack, bool out_in_host = false) {
     const int S = p->c.subgrid_size;
     CK(p->d_subgrids.ensure(sizeof(float2) * S * S * std::max<size_t>(1, p->dsub.size())));
+    TRY(ensure_gaps(p));
+    const int64_t ngaps = static_cast<int64_t>(p->gaps.size() / 2);
+    ZeroSide z{p};
+    if (!out_in_host) TRY(z.fork());
     {
         StageScope t(p, P9IDG_STAGE_SPLIT_SUBGRID_FFT);
         SubgridOpArgs a = subgrid_args(p);
@@ -566,16 +612,10 @@ p9idg_status run_degrid(p9idg_plan *p, const float2 *d_grid, bool grid_shifted, 
         a.wstack = wstack;
         CK(launch_split_subgrid_fft(a, p->stream));
     }
+    if (!out_in_host) CK(launch_zero_ranges_beside(d_vis, out_c128, p->d_gaps.as<int64_t>(), ngaps, p->zside));
     {
         StageScope t(p, P9IDG_STAGE_DEGRIDDER);
-        const size_t nvis = static_cast<size_t>(p->nbl) * p->nt * p->nch;
-        if (zero_gaps && out_c128) {
-            TRY(ensure_gaps(p));
-            CK(launch_zero_ranges(static_cast<double2 *>(d_vis), p->d_gaps.as<int64_t>(),
-                                  static_cast<int64_t>(p->gaps.size() / 2), p->stream));
-        } else {
-            CK(cudaMemsetAsync(d_vis, 0, nvis * (out_c128 ? sizeof(double2) : sizeof(float2)), p->stream));
-        }
+        if (out_in_host) CK(launch_zero_ranges(d_vis, out_c128, p->d_gaps.as<int64_t>(), ngaps, p->stream));
         GridderArgs a = gridder_args(p);
         a.items = p->d_ditems.as<WorkItem>();
         a.nitems = static_cast<int32_t>(p->ditems.size());
@@ -589,6 +629,7 @@ p9idg_status run_degrid(p9idg_plan *p, const float2 *d_grid, bool grid_shifted, 
             CK(launch_degridder_fp32(a, p->stream));
         }
     }
+    if (!out_in_host) TRY(z.join());
     return P9IDG_OK;
 }
 
@@ -878,11 +919,18 @@ p9idg_status host_grid_common(p9idg_plan *p, const double *vis, const double *uv
             const int32_t *subl = p->d_sub_lyr.as<int32_t>();
             const int32_t nmi = p->lyr_minor_items, nms = p->lyr_minor_subs;
             const size_t major = static_cast<size_t>(p->lyr_major);
-            int clear = static_cast<int>(nl);  // the first add zeroes every layer
+            // every layer is zeroed beside the first gridder launch, before the first add
+            ZeroSide z{p};
+            TRY(z.fork());
+            auto zero_layers = [&]() -> p9idg_status {
+                if (z.joined) return P9IDG_OK;
+                CK(launch_zero_c64_beside(layers, static_cast<int64_t>(nl * nn), p->zside));
+                return z.join();
+            };
             if (nmi > 0 || nms > 0) {
                 TRY(grid_items(p, vis, true, items, nmi));
-                TRY(add_subgrids(p, layers, true, subl, nms, clear));
-                clear = 0;
+                TRY(zero_layers());
+                TRY(add_subgrids(p, layers, true, subl, nms));
                 CK(cudaEventRecord(p->ev_mid, p->stream));
                 CK(cudaStreamWaitEvent(p->side, p->ev_mid, 0));
                 for (size_t k = 0; k < nl; k++)
@@ -894,14 +942,15 @@ p9idg_status host_grid_common(p9idg_plan *p, const double *vis, const double *uv
             const int N = p->c.grid_size;
             for (size_t b = 0; b + 1 < br.size(); b++) {
                 TRY(grid_items(p, vis, true, items + nmi + bi[b], bi[b + 1] - bi[b]));
-                TRY(add_subgrids(p, layers, true, subl + nms + bs[b], bs[b + 1] - bs[b], clear));
-                clear = 0;
+                TRY(zero_layers());
+                TRY(add_subgrids(p, layers, true, subl + nms + bs[b], bs[b + 1] - bs[b]));
                 // the band's final rows cross the link while the next band grids
                 CK(cudaEventRecord(p->ev_mid, p->stream));
                 CK(cudaStreamWaitEvent(p->side, p->ev_mid, 0));
                 TRY(layer_rows_to_host(layers + major * nn, N, br[b], br[b + 1], out128 + major * nn,
                                        stage(major), pinned, p->side));
             }
+            TRY(zero_layers());  // (done by then: the busiest layer has at least one band)
         }
         CK(cudaEventRecord(p->ev_join, p->side));
         CK(cudaStreamWaitEvent(p->stream, p->ev_join, 0));
@@ -1356,6 +1405,9 @@ void p9idg_plan_destroy(p9idg_plan *plan) {
         if (plan->ev_fork) cudaEventDestroy(plan->ev_fork);
         if (plan->ev_join) cudaEventDestroy(plan->ev_join);
         if (plan->ev_mid) cudaEventDestroy(plan->ev_mid);
+        if (plan->zside) cudaStreamDestroy(plan->zside);
+        if (plan->ev_zfork) cudaEventDestroy(plan->ev_zfork);
+        if (plan->ev_zjoin) cudaEventDestroy(plan->ev_zjoin);
         if (plan->own_stream) cudaStreamDestroy(plan->own_stream);
     }
     delete plan;

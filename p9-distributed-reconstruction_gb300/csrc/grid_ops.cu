@@ -5,6 +5,7 @@
 // roofline denominator.  All are grid-stride loops sized to the SM count.
 
 #include <algorithm>
+#include <cstdint>
 #include <type_traits>
 
 #include "kernels.cuh"
@@ -13,7 +14,7 @@ namespace p9idg {
 
 namespace {
 
-int grid_blocks(int64_t n, int threads) {
+int sm_count() {
     static int sms = 0;
     if (sms == 0) {
         int dev = 0;
@@ -21,6 +22,11 @@ int grid_blocks(int64_t n, int threads) {
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         if (sms <= 0) sms = 132;
     }
+    return sms;
+}
+
+int grid_blocks(int64_t n, int threads) {
+    const int sms = sm_count();
     const int64_t want = (n + threads - 1) / threads;
     return static_cast<int>(want < static_cast<int64_t>(sms) * 8 ? (want > 0 ? want : 1) : sms * 8);
 }
@@ -173,11 +179,30 @@ cudaError_t launch_shift_convert(const double2 *in, int n, float2 *out64, double
     return cudaGetLastError();
 }
 
-// Zeroes the listed index ranges (pairs start, count) of a complex128 array.
-__global__ void zero_ranges_kernel(double2 *__restrict__ out, const int64_t *__restrict__ ranges, int64_t nranges) {
+// Zeroes the listed index ranges (pairs start, count) of a complex64 or complex128 array.
+template <typename T>
+__global__ void zero_ranges_kernel(T *__restrict__ out, const int64_t *__restrict__ ranges, int64_t nranges) {
+    T z;
+    z.x = 0;
+    z.y = 0;
     for (int64_t r = blockIdx.x; r < nranges; r += gridDim.x) {
         const int64_t start = ranges[2 * r], count = ranges[2 * r + 1];
-        for (int64_t j = threadIdx.x; j < count; j += blockDim.x) out[start + j] = make_double2(0.0, 0.0);
+        for (int64_t j = threadIdx.x; j < count; j += blockDim.x) out[start + j] = z;
+    }
+}
+
+// Zeroes n8 8-byte words from an 8-byte aligned address, in 16-byte stores from the first 16-byte
+// boundary on (the word before it, if any, and an odd last word by single stores).
+__global__ void zero_words_kernel(uint2 *__restrict__ out, int64_t n8) {
+    const int64_t head = (reinterpret_cast<uintptr_t>(out) & 15) != 0 && n8 > 0 ? 1 : 0;
+    const int64_t n16 = (n8 - head) / 2;
+    uint4 *body = reinterpret_cast<uint4 *>(out + head);
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n16;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+        body[i] = make_uint4(0u, 0u, 0u, 0u);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        if (head) out[0] = make_uint2(0u, 0u);
+        if ((n8 - head) & 1) out[n8 - 1] = make_uint2(0u, 0u);
     }
 }
 
@@ -213,10 +238,33 @@ cudaError_t launch_zero_c128(double2 *out, int64_t count, cudaStream_t st) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_zero_ranges(double2 *out, const int64_t *ranges, int64_t nranges, cudaStream_t st) {
+cudaError_t launch_zero_ranges(void *out, bool c128, const int64_t *ranges, int64_t nranges, cudaStream_t st) {
     if (nranges == 0) return cudaSuccess;
     const unsigned blocks = static_cast<unsigned>(std::min<int64_t>(nranges, 8192));
-    zero_ranges_kernel<<<blocks, 256, 0, st>>>(out, ranges, nranges);
+    if (c128)
+        zero_ranges_kernel<double2><<<blocks, 256, 0, st>>>(static_cast<double2 *>(out), ranges, nranges);
+    else
+        zero_ranges_kernel<float2><<<blocks, 256, 0, st>>>(static_cast<float2 *>(out), ranges, nranges);
+    return cudaGetLastError();
+}
+
+// The two zero-fills that run beside the gridder or degridder (on a high-priority stream): one CTA
+// of 128 threads per SM, which fits in the registers, threads and shared memory that two
+// tensor-core gridder or degridder CTAs leave free on an SM, so it neither waits for their items
+// nor takes an SM from them.
+cudaError_t launch_zero_ranges_beside(void *out, bool c128, const int64_t *ranges, int64_t nranges, cudaStream_t st) {
+    if (nranges == 0) return cudaSuccess;
+    const unsigned blocks = static_cast<unsigned>(std::min<int64_t>(nranges, sm_count()));
+    if (c128)
+        zero_ranges_kernel<double2><<<blocks, 128, 0, st>>>(static_cast<double2 *>(out), ranges, nranges);
+    else
+        zero_ranges_kernel<float2><<<blocks, 128, 0, st>>>(static_cast<float2 *>(out), ranges, nranges);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_zero_c64_beside(float2 *out, int64_t count, cudaStream_t st) {
+    if (count == 0) return cudaSuccess;
+    zero_words_kernel<<<sm_count(), 128, 0, st>>>(reinterpret_cast<uint2 *>(out), count);
     return cudaGetLastError();
 }
 

@@ -159,6 +159,45 @@ def test_device_api_matches_host_api(need_gpu):
     plan.set_stream(0)
 
 
+@pytest.mark.parametrize("mode,tol", [(pkg.MODE_FP32, TOL), (pkg.MODE_TC_BF16X3, 1e-4)], ids=["fp32", "tc_bf16x3"])
+def test_device_outputs_fully_written(need_gpu, mode, tol):
+    """The device entry points write every element of their outputs, which start as NaN here: the
+    w layers are zero-filled beside the gridder, and the visibilities no subgrid covers (quirk P1
+    drops 18 % of this observation's samples) beside the degridder, which writes all the others.
+    The layers start 8 bytes past a 16-byte boundary and hold an odd number of elements (N = 3071),
+    so the fill's single first and last words are exercised too."""
+    torch = pytest.importorskip("torch")
+    obs, c, cd, part, subs = _setup("meerkat_3072", dict(n_ant=10, nt=300, nch=16), grid_size=3071)
+    plan = part.plan
+    assert plan.set_mode(mode) == mode
+    plan.set_stream(torch.cuda.current_stream().cuda_stream)
+    N, W = cd["grid_size"], cd["wlayer_count"]
+    nan = complex(float("nan"), float("nan"))
+    d_vis = torch.from_numpy(obs.vis.astype(np.complex64)).cuda()
+    buf = torch.full((W * N * N + 1,), nan, dtype=torch.complex64, device="cuda")
+    d_layers = buf[1:]
+    assert d_layers.data_ptr() % 16 == 8
+    plan.grid_w_device(d_vis.data_ptr(), d_layers.data_ptr())
+    plan.synchronize()
+    layers = d_layers.cpu().numpy().reshape(W, N, N)
+    assert np.isfinite(layers).all() and np.isnan(buf[0].item().real)  # the word before is untouched
+    assert rel_l2(layers, oracle.idg_grid_w(cd, subs, obs.vis, obs.uvw, obs.frequencies)) < tol
+    model = oracle.fft_forward_float(obs.model_image[:N, :N].astype(np.float32))
+    d_grid = torch.from_numpy(model.astype(np.complex64)).cuda()
+    d_out = torch.full_like(d_vis, nan)
+    plan.degrid_w_device(d_grid.data_ptr(), d_out.data_ptr())
+    plan.synchronize()
+    out = d_out.cpu().numpy()
+    covered = np.zeros(obs.vis.shape[:2], bool)
+    for s in subs:
+        covered[s["baseline_idx"], s["time_sample_start"]:s["time_sample_start"] + s["time_sample_count"]] = True
+    assert (~covered).any() and np.isfinite(out).all()
+    assert not out[~covered].any()
+    ref_v, _ = oracle.idg_degrid(cd, subs, model, obs.uvw, obs.frequencies, wstack=True)
+    assert rel_l2(out, ref_v) < tol
+    plan.set_stream(0)
+
+
 @pytest.mark.parametrize("mode", [pkg.MODE_FP32, pkg.MODE_TC_BF16X3], ids=["fp32", "tc_bf16x3"])
 def test_uvw_kept_on_the_device(need_gpu, mode):
     """uvw=None (NULL in the C ABI): the uvw the partition was made from, which the plan keeps on
