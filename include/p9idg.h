@@ -197,8 +197,7 @@ p9idg_status p9idg_fft_shift(void *array, int32_t n, int32_t elem_bytes);
 /* These run asynchronously on the plan's stream; p9idg_synchronize waits and
  * reports kernel-side check failures.  uvw and frequencies are the plan's.  The zeroing of an
  * output runs on a second stream of the plan, forked from the plan's stream and joined back into
- * it within the call, so all of a call's work is ordered on the plan's stream (and may be
- * captured from it into a CUDA graph, once the plan's first call has set it up). */
+ * it within the call, so all of a call's work is ordered on the plan's stream. */
 
 /* Gridder + subgrid IFFT + w-stack adder: vis complex64[nbl][nt][nch] -> layers complex64[W][N][N]
  * (already FFT.Shift-ed, as IDG.GridW returns them).  The layers are overwritten. */
