@@ -251,14 +251,14 @@ cudaError_t launch_zero_ranges(void *out, bool c128, const int64_t *ranges, int6
 // The two zero-fills that run beside the gridder or degridder (on a high-priority stream): CTAs of
 // 128 threads, which fit in the registers, threads and shared memory that two tensor-core gridder
 // or degridder CTAs leave free on an SM, so they neither wait for those kernels' items nor take an
-// SM from them; one per four SMs.  Beside the 3072^2 gridder the 604 MB layer fill slowed it by
+// SM from them.  Measured on the 3072^2 workload: the 604 MB layer fill slowed the gridder by
 // 0.023 ms with one CTA per four SMs, 0.032 ms with one per SM, and 0.070 ms as a cudaMemsetAsync
-// on the same stream; it ends well before the gridder does.
-static int beside_blocks() { return std::max(1, sm_count() / 4); }
-
+// on the same stream, ending well before the gridder does; the 180 MB fill of the uncovered
+// visibilities, over 823 ranges, cost splitter + degridder 0.010 ms less with one CTA per SM than
+// with one per four SMs.
 cudaError_t launch_zero_ranges_beside(void *out, bool c128, const int64_t *ranges, int64_t nranges, cudaStream_t st) {
     if (nranges == 0) return cudaSuccess;
-    const unsigned blocks = static_cast<unsigned>(std::min<int64_t>(nranges, beside_blocks()));
+    const unsigned blocks = static_cast<unsigned>(std::min<int64_t>(nranges, sm_count()));
     if (c128)
         zero_ranges_kernel<double2><<<blocks, 128, 0, st>>>(static_cast<double2 *>(out), ranges, nranges);
     else
@@ -268,7 +268,7 @@ cudaError_t launch_zero_ranges_beside(void *out, bool c128, const int64_t *range
 
 cudaError_t launch_zero_c64_beside(float2 *out, int64_t count, cudaStream_t st) {
     if (count == 0) return cudaSuccess;
-    zero_words_kernel<<<beside_blocks(), 128, 0, st>>>(reinterpret_cast<uint2 *>(out), count);
+    zero_words_kernel<<<std::max(1, sm_count() / 4), 128, 0, st>>>(reinterpret_cast<uint2 *>(out), count);
     return cudaGetLastError();
 }
 

@@ -110,7 +110,7 @@ cudaError_t launch_shift_convert(const double2 *in, int n, float2 *out64, double
 cudaError_t launch_c64_to_c128(const float2 *in, int64_t count, double2 *out, cudaStream_t st);
 // zeroes the (start, count) index ranges of a complex64 or complex128 array
 cudaError_t launch_zero_ranges(void *out, bool c128, const int64_t *ranges, int64_t nranges, cudaStream_t st);
-// zero-fills to run beside a tensor-core gridder or degridder: one 128-thread CTA per four SMs
+// zero-fills to run beside a tensor-core gridder or degridder: CTAs of 128 threads, at most one per SM
 cudaError_t launch_zero_ranges_beside(void *out, bool c128, const int64_t *ranges, int64_t nranges, cudaStream_t st);
 cudaError_t launch_zero_c64_beside(float2 *out, int64_t count, cudaStream_t st);
 cudaError_t launch_zero_c128(double2 *out, int64_t count, cudaStream_t st);
